@@ -1,0 +1,203 @@
+/*
+ * abea.h — C ABI of the GB300-native Adaptive Banded Event Alignment (ABEA).
+ *
+ * The library replaces f5c's CPU `align()` (prototype in the reference at
+ * GPU/f5cmisc.h:48-50) and its batch GPU entry `align_cuda(core, db)`
+ * (GPU/f5cmisc.h:99-102), whose OpenCL re-implementation in the reference is
+ * `align_ocl(core, db)` (GPU/align_cuda.c:391-943).  All computation runs in
+ * hand-written sm_103a CUDA kernels; there is no CPU fallback.  Every entry
+ * point takes plain pointers and sizes and never exits the process: failures
+ * are reported as negative `abea_status_t` codes plus a thread-local message
+ * (`abea_last_error`).
+ *
+ * Data layouts are byte-identical to the reference's shared types
+ * (GPU/f5c.h:113-181) on LP64 targets (x86-64 and aarch64):
+ *   abea_event_t        == event_t        (24 B: u64 start, f32 length/mean/stdv, 4 B pad)
+ *   abea_event_table_t  == event_table    (n, start, end, event*)
+ *   abea_model_t        == model_t        (12 B, CACHED_LOG layout)
+ *   abea_scalings_t     == scalings_t     (16 B, CACHED_LOG layout)
+ *   abea_aligned_pair_t == AlignedPair    (8 B)
+ *   abea_event_kmer_pair_t == EventKmerPair (8 B)
+ */
+#ifndef ABEA_H
+#define ABEA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Algorithm constants: KMER_SIZE, NUM_KMER, ALN_BANDWIDTH (GPU/f5c.h:26-30). */
+#define ABEA_KMER_SIZE 6
+#define ABEA_NUM_KMER 4096
+#define ABEA_BANDWIDTH 100
+
+/* ---- shared types (GPU/f5c.h:113-181) ---------------------------------- */
+typedef struct {
+    uint64_t start;
+    float length;
+    float mean;
+    float stdv;
+} abea_event_t;
+
+typedef struct {
+    size_t n;
+    size_t start;
+    size_t end;
+    abea_event_t *event;
+} abea_event_table_t;
+
+typedef struct {
+    float level_mean;
+    float level_stdv;
+    float level_log_stdv;
+} abea_model_t;
+
+typedef struct {
+    float scale;
+    float shift;
+    float var;
+    float log_var;
+} abea_scalings_t;
+
+typedef struct {
+    int32_t ref_pos;
+    int32_t read_pos;
+} abea_aligned_pair_t;
+
+typedef struct {
+    int32_t event_idx;
+    int32_t kmer_idx;
+} abea_event_kmer_pair_t;
+
+/* ---- status codes ------------------------------------------------------ */
+typedef enum {
+    ABEA_OK = 0,
+    ABEA_ERR_INVALID_ARG = -1,   /* null pointer, negative size, non-finite model */
+    ABEA_ERR_CAPACITY = -2,      /* an alignment path longer than its output slot */
+    ABEA_ERR_OUT_OF_MEMORY = -3, /* device or pinned-host allocation failed */
+    ABEA_ERR_CUDA = -4,          /* a CUDA runtime call failed */
+    ABEA_ERR_TIMEOUT = -5,       /* a bounded device-side wait gave up */
+    ABEA_ERR_NO_DEVICE = -6,     /* no CUDA device, or the library's kernels do not run on it */
+    ABEA_ERR_INTERNAL = -7,      /* a device-side consistency check failed */
+    ABEA_ERR_UNDEFINED = -8      /* the reference's traceback would read outside the read's band
+                                    arrays for this read; no defined answer exists */
+} abea_status_t;
+
+/* Execution forms.
+ *  PLAIN   — the reference's structure: three kernels (pre, core, post) launched
+ *            one after the other, one thread block per read, full score and
+ *            trace matrices in HBM (GPU/align_cuda.c:680-850).
+ *  BATCHED — one persistent kernel per stage pulling reads longest-first from a
+ *            device work queue, several threads-per-band shapes chosen per
+ *            length bucket, all three stages replayed as one CUDA graph. */
+typedef enum { ABEA_MODE_PLAIN = 0, ABEA_MODE_BATCHED = 1 } abea_mode_t;
+
+/* Context options (abea_ctx_set_option). */
+typedef enum {
+    ABEA_OPT_MODE = 0,          /* abea_mode_t */
+    ABEA_OPT_STORE_SCORES = 1,  /* 1: keep every band's scores in HBM (reference layout, GPU/align_cuda.c:573-577) */
+    ABEA_OPT_USE_GRAPH = 2,     /* BATCHED only: 1 = replay the three stages as one CUDA graph */
+    ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide (4-warp) shape; 0 = autotuned */
+    ABEA_OPT_SPIN_LIMIT = 4     /* upper bound on any device-side wait, in polling iterations */
+} abea_option_t;
+
+typedef struct abea_ctx abea_ctx_t;
+typedef struct abea_batch abea_batch_t;
+
+/* Stage timings of the most recent run of a batch, milliseconds (CUDA events on
+ * the context's stream). */
+typedef struct {
+    float pre_ms;
+    float core_ms;
+    float post_ms;
+    float total_ms;
+    float h2d_ms;
+    float d2h_ms;
+    int32_t kernel_launches;
+} abea_timing_t;
+
+/* ---- context ------------------------------------------------------------ */
+/* Creates a context (one CUDA stream and its scratch buffers) on `device`. */
+abea_status_t abea_ctx_create(abea_ctx_t **ctx, int device, abea_mode_t mode);
+void abea_ctx_destroy(abea_ctx_t *ctx);
+abea_status_t abea_ctx_set_option(abea_ctx_t *ctx, abea_option_t opt, int64_t value);
+abea_status_t abea_ctx_get_option(abea_ctx_t *ctx, abea_option_t opt, int64_t *value);
+/* Message of the last failure on the calling thread ("" if none). */
+const char *abea_last_error(void);
+const char *abea_status_string(abea_status_t status);
+/* Library version string. */
+const char *abea_version(void);
+
+/* ---- drop-in single-read entry: f5c align() (GPU/f5cmisc.h:48-50) -------
+ * Same arguments, same meaning: `out_2` is caller-allocated; f5c sizes it at
+ * 2*events.n pairs (GPU/align_cuda.c:496).  Returns the number of AlignedPairs
+ * written, 0 when the alignment failed the reference's quality checks
+ * (GPU/align_cuda.cl:856-882), or a negative abea_status_t on error.
+ * `sample_rate` is unused by the algorithm, as in the reference.
+ * Thread-safe: each calling thread gets its own context and stream. */
+int32_t abea_align(abea_aligned_pair_t *out_2, char *sequence, int32_t sequence_len,
+                   abea_event_table_t events, abea_model_t *models, abea_scalings_t scaling,
+                   float sample_rate);
+
+/* Same as abea_align with an explicit output capacity (in pairs). */
+int32_t abea_align_cap(abea_aligned_pair_t *out_2, int32_t out_capacity, const char *sequence,
+                       int32_t sequence_len, const abea_event_t *events, int32_t n_events,
+                       const abea_model_t *models, abea_scalings_t scaling);
+
+/* ---- batch entry: align_cuda(core, db) / align_ocl(core, db) ------------
+ * Host arrays in the reference's flattened layout (GPU/align_cuda.c:432-497):
+ *   read[read_ptr[i] .. read_ptr[i]+read_len[i])  bases of read i (NUL separators allowed)
+ *   event_table[event_ptr[i] .. +n_events[i])     events of read i
+ *   scalings[i], model[4096]
+ * Outputs (host): event_align_pairs[2*event_ptr[i] ...] gets read i's pairs
+ * (capacity 2*n_events[i], as in the reference), n_event_align_pairs[i] its
+ * count (0 = failed QC; negative = per-read abea_status_t).  Host->device and
+ * device->host copies happen inside the call. */
+abea_status_t abea_align_batch(abea_ctx_t *ctx, int32_t n_reads, const char *read,
+                               const int64_t *read_ptr, const int32_t *read_len,
+                               const abea_event_t *event_table, const int64_t *event_ptr,
+                               const int32_t *n_events, const abea_scalings_t *scalings,
+                               const abea_model_t *model, abea_aligned_pair_t *event_align_pairs,
+                               int32_t *n_event_align_pairs);
+
+/* ---- device-resident batches --------------------------------------------
+ * abea_batch_create copies a batch (same host layout as abea_align_batch) into
+ * HBM once; abea_batch_run aligns it on the context's stream (asynchronous);
+ * abea_batch_sync waits; abea_batch_results copies results to the host. */
+abea_status_t abea_batch_create(abea_ctx_t *ctx, int32_t n_reads, const char *read,
+                                const int64_t *read_ptr, const int32_t *read_len,
+                                const abea_event_t *event_table, const int64_t *event_ptr,
+                                const int32_t *n_events, const abea_scalings_t *scalings,
+                                const abea_model_t *model, abea_batch_t **batch);
+abea_status_t abea_batch_run(abea_ctx_t *ctx, abea_batch_t *batch);
+abea_status_t abea_batch_sync(abea_ctx_t *ctx);
+abea_status_t abea_batch_results(abea_ctx_t *ctx, abea_batch_t *batch,
+                                 abea_aligned_pair_t *event_align_pairs, int32_t *n_event_align_pairs);
+abea_status_t abea_batch_timing(abea_ctx_t *ctx, abea_batch_t *batch, abea_timing_t *timing);
+void abea_batch_destroy(abea_batch_t *batch);
+
+/* Band matrices of one read after a run, converted to the reference layout
+ * (GPU/align_cuda.c:573-583): bands[n_bands*100] scores (needs
+ * ABEA_OPT_STORE_SCORES=1, else NULL must be passed), trace[n_bands*100]
+ * backpointers (0=D, 1=U, 2=L), band_lower_left[n_bands].  n_bands =
+ * n_events + n_kmers + 2.  For tests and debugging. */
+abea_status_t abea_batch_read_bands(abea_ctx_t *ctx, abea_batch_t *batch, int32_t read_index,
+                                    float *bands, uint8_t *trace,
+                                    abea_event_kmer_pair_t *band_lower_left);
+
+/* Per-read best end score (the maximum of the last k-mer column plus trim
+ * penalties, GPU/align_cuda.cl:722-746) of the last run, host array [n_reads]. */
+abea_status_t abea_batch_best_scores(abea_ctx_t *ctx, abea_batch_t *batch, float *best_scores);
+
+/* Number of band cells whose exact double-rounded scores were taken from the
+ * FP64 slow path during the last run (diagnostic). */
+abea_status_t abea_batch_slow_cells(abea_ctx_t *ctx, abea_batch_t *batch, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ABEA_H */

@@ -1,0 +1,502 @@
+/*
+ * abea_oracle.c — CPU oracle for ABEA.  TEST INFRASTRUCTURE ONLY: the checker
+ * for tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.  The
+ * product library never links or calls it.
+ *
+ * Restates, in plain C, the reference's algorithm for f5c's align():
+ *   fill  : FPGA/code/device/align_swi.cl:184-503 (single-work-item kernel)
+ *   post  : FPGA/code/host/src/align_swi.cpp:1093-1314 (best end, traceback,
+ *           reverse, QC), with the double-precision sum_emission of the
+ *           GPU NDRange post kernel GPU/align_cuda.cl:713-714 (f5c's form).
+ * Compile with -ffp-contract=off: the reference's arithmetic has no fused
+ * multiply-add, and contraction changes AlignedPairs (142/143 on the dump).
+ */
+#include "abea_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define W ABEA_BANDWIDTH
+#define HALF_W (ABEA_BANDWIDTH / 2)
+#define FROM_D 0
+#define FROM_U 1
+#define FROM_L 2
+#define MAX_GAP_THRESHOLD 50        /* GPU/align_cuda.cl:128 */
+#define MIN_AVG_LOG_EMISSION (-5.0) /* GPU/align_cuda.cl:133 */
+#define LOG_INV_SQRT_2PI (-0.918938f) /* GPU/align_cuda.cl:66 */
+
+/* A/C/G/T -> 0..3, anything else 0 (GPU/align_cuda.cl:22-35). */
+static inline uint32_t base_rank(char b) {
+    switch (b) {
+    case 'A': return 0;
+    case 'C': return 1;
+    case 'G': return 2;
+    case 'T': return 3;
+    default: return 0;
+    }
+}
+
+/* First base most significant: rank = sum_j rank(s[j]) << 2*(5-j)
+ * (GPU/align_cuda.cl:39-51). */
+uint32_t oracle_kmer_rank(const char *s) {
+    uint32_t r = 0;
+    for (int j = 0; j < ABEA_KMER_SIZE; ++j) r = (r << 2) | base_rank(s[j]);
+    return r;
+}
+
+/* log_probability_match_r9 + log_normal_pdf in float, reference order:
+ *   gp_mean = scale*level_mean + shift; a = (x - gp_mean)/gp_stdv;
+ *   lp = (log_inv_sqrt_2pi - gp_log_stdv) + ((-0.5f*a)*a)
+ * gp_stdv ignores scaling.var in the reference (GPU/align_cuda.cl:95,509,
+ * align_swi.cl:99); ORACLE_VAR_AWARE applies var like nanopolish does. */
+float oracle_emission(float x, const abea_model_t *m, abea_scalings_t sc, uint32_t flags) {
+    float gp_mean = sc.scale * m->level_mean;
+    gp_mean = gp_mean + sc.shift;
+    float gp_stdv = m->level_stdv;
+    float gp_log_stdv;
+    if (flags & ORACLE_LOG_UNCACHED)
+        gp_log_stdv = (float)log((double)m->level_stdv);
+    else
+        gp_log_stdv = m->level_log_stdv;
+    if (flags & ORACLE_VAR_AWARE) {
+        gp_stdv = gp_stdv * sc.var;
+        gp_log_stdv = gp_log_stdv + sc.log_var;
+    }
+    float a = (x - gp_mean) / gp_stdv;
+    float t = -0.5f * a;
+    t = t * a;
+    float c = LOG_INV_SQRT_2PI - gp_log_stdv;
+    return c + t;
+}
+
+float oracle_add3(float a, double b, float c) {
+    double t = (double)a + b;
+    t = t + (double)c;
+    return (float)t;
+}
+
+int64_t oracle_n_bands(int32_t seq_len, int32_t n_events) {
+    return (int64_t)n_events + (int64_t)(seq_len - ABEA_KMER_SIZE + 1) + 2;
+}
+
+typedef struct {
+    double lp_skip, lp_stay, lp_step, lp_trim;
+} penalties_t;
+
+/* Transition log-probabilities, double (align_swi.cl:233-250). */
+static penalties_t make_penalties(int32_t n_events, int32_t n_kmers) {
+    penalties_t p;
+    double events_per_kmer = (double)n_events / n_kmers;
+    double p_stay = 1 - (1 / (events_per_kmer + 1));
+    p.lp_skip = log(1e-10);
+    p.lp_stay = log(p_stay);
+    p.lp_step = log(1.0 - exp(p.lp_skip) - exp(p.lp_stay));
+    p.lp_trim = log(0.01);
+    return p;
+}
+
+#define BAND(b, o) bands[(size_t)(b) * W + (size_t)(o)]
+#define TRACE(b, o) trace[(size_t)(b) * W + (size_t)(o)]
+#define VALID(o) ((o) >= 0 && (o) < W)
+
+int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq, int32_t seq_len,
+                     const abea_event_t *events, int32_t n_events, const abea_model_t *model,
+                     abea_scalings_t sc, uint32_t flags, oracle_debug_t *dbg) {
+    if (dbg) {
+        dbg->best_score = -INFINITY;
+        dbg->best_event = 0;
+        dbg->sum_emission = 0.0;
+        dbg->path_len = 0;
+        dbg->max_gap = 0;
+    }
+    if (!out || !seq || !model || (n_events > 0 && !events) || n_events < 0 || seq_len < 0)
+        return ABEA_ERR_INVALID_ARG;
+    int32_t n_kmers = seq_len - ABEA_KMER_SIZE + 1;
+    /* The reference has no defined result for these (division by zero /
+     * reading events[0] of an empty table); the library returns 0 pairs. */
+    if (n_kmers <= 0 || n_events <= 0) return 0;
+
+    penalties_t pen = make_penalties(n_events, n_kmers);
+    int64_t n_bands = (int64_t)n_events + n_kmers + 2;
+
+    uint32_t *ranks = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n_kmers);
+    float *bands = (float *)malloc(sizeof(float) * (size_t)n_bands * W);
+    uint8_t *trace = (uint8_t *)calloc((size_t)n_bands * W, 1);
+    abea_event_kmer_pair_t *bll =
+        (abea_event_kmer_pair_t *)malloc(sizeof(abea_event_kmer_pair_t) * (size_t)n_bands);
+    if (!ranks || !bands || !trace || !bll) {
+        free(ranks); free(bands); free(trace); free(bll);
+        return ABEA_ERR_OUT_OF_MEMORY;
+    }
+    for (int32_t k = 0; k < n_kmers; ++k) ranks[k] = oracle_kmer_rank(seq + k);
+    for (int64_t i = 0; i < n_bands * W; ++i) bands[i] = -INFINITY;
+
+    /* ---- fill (align_swi.cl:305-503) ---- */
+    bll[0].event_idx = HALF_W - 1;
+    bll[0].kmer_idx = -1 - HALF_W;
+    bll[1].event_idx = bll[0].event_idx + 1;
+    bll[1].kmer_idx = bll[0].kmer_idx;
+    BAND(0, -1 - bll[0].kmer_idx) = 0.0f;            /* start cell (e=-1,k=-1) */
+    BAND(1, bll[1].event_idx - 0) = (float)pen.lp_trim; /* first event trimmed */
+    TRACE(1, bll[1].event_idx - 0) = FROM_U;
+
+    for (int64_t b = 2; b < n_bands; ++b) {
+        float ll = BAND(b - 1, 0);
+        float ur = BAND(b - 1, W - 1);
+        int right;
+        if (ll == -INFINITY && ur == -INFINITY)
+            right = (int)(b & 1); /* alternate when both ends are out of band */
+        else
+            right = ll < ur; /* Suzuki-Kasahara rule */
+        abea_event_kmer_pair_t cur = bll[b - 1];
+        if (right)
+            cur.kmer_idx += 1;
+        else
+            cur.event_idx += 1;
+        bll[b] = cur;
+
+        int trim_offset = -1 - cur.kmer_idx;
+        if (VALID(trim_offset)) {
+            int32_t e = cur.event_idx - trim_offset;
+            if (e >= 0 && e < n_events) {
+                BAND(b, trim_offset) = (float)(pen.lp_trim * (e + 1));
+                TRACE(b, trim_offset) = FROM_U;
+            } else {
+                BAND(b, trim_offset) = -INFINITY;
+            }
+        }
+
+        int lo = -cur.kmer_idx;
+        int t = cur.event_idx - (n_events - 1);
+        if (t > lo) lo = t;
+        if (lo < 0) lo = 0;
+        int hi = n_kmers - cur.kmer_idx;
+        t = cur.event_idx + 1;
+        if (t < hi) hi = t;
+        if (W < hi) hi = W;
+
+        const abea_event_kmer_pair_t p1 = bll[b - 1], p2 = bll[b - 2];
+        for (int o = lo; o < hi; ++o) {
+            int e = cur.event_idx - o;
+            int k = cur.kmer_idx + o;
+            int o_up = p1.event_idx - (e - 1);
+            int o_left = (k - 1) - p1.kmer_idx;
+            int o_diag = (k - 1) - p2.kmer_idx;
+            float up = VALID(o_up) ? BAND(b - 1, o_up) : -INFINITY;
+            float left = VALID(o_left) ? BAND(b - 1, o_left) : -INFINITY;
+            float diag = VALID(o_diag) ? BAND(b - 2, o_diag) : -INFINITY;
+            float em = oracle_emission(events[e].mean, &model[ranks[k]], sc, flags);
+            /* float + double + float evaluated in double, rounded once to float */
+            float s_d = oracle_add3(diag, pen.lp_step, em);
+            float s_u = oracle_add3(up, pen.lp_stay, em);
+            float s_l = (float)((double)left + pen.lp_skip);
+            float best = s_d;
+            uint8_t from = FROM_D;
+            best = s_u > best ? s_u : best;
+            from = best == s_u ? FROM_U : from;
+            best = s_l > best ? s_l : best;
+            from = best == s_l ? FROM_L : from;
+            BAND(b, o) = best;
+            TRACE(b, o) = from;
+        }
+    }
+
+    /* ---- best end on the last k-mer column (align_swi.cpp:1149-1171) ---- */
+    float max_score = -INFINITY;
+    int32_t cur_e = 0;
+    int32_t cur_k = n_kmers - 1;
+    for (int32_t e = 0; e < n_events; ++e) {
+        int64_t b = (int64_t)e + cur_k + 2;
+        int o = bll[b].event_idx - e;
+        if (VALID(o)) {
+            float s = (float)((double)BAND(b, o) + (n_events - e) * pen.lp_trim);
+            if (s > max_score) {
+                max_score = s;
+                cur_e = e;
+            }
+        }
+    }
+    if (dbg) {
+        dbg->best_score = max_score;
+        dbg->best_event = cur_e;
+    }
+
+    /* ---- traceback (align_swi.cpp:1178-1236) ---- */
+    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0;
+    double sum_em = 0.0;
+    float sum_em_f = 0.0f;
+    double n_aligned = 0.0;
+    while (cur_k >= 0 && cur_e >= 0) {
+        if (n_out >= out_cap) {
+            status = ABEA_ERR_CAPACITY;
+            break;
+        }
+        out[n_out].ref_pos = cur_k;
+        out[n_out].read_pos = cur_e;
+        n_out++;
+        float em = oracle_emission(events[cur_e].mean, &model[ranks[cur_k]], sc, flags);
+        sum_em += (double)em;
+        sum_em_f += em;
+        n_aligned += 1;
+        int64_t b = (int64_t)cur_e + cur_k + 2;
+        /* The reference indexes the flat band array: an offset outside the
+         * band reads a neighbouring band's row.  Within the read's own rows
+         * that is reproduced; beyond them the reference has no defined answer. */
+        int64_t idx = b * W + (int64_t)(bll[b].event_idx - cur_e);
+        if (idx < 0 || idx >= n_bands * W) {
+            status = ABEA_ERR_UNDEFINED;
+            break;
+        }
+        uint8_t from = trace[idx];
+        if (from == FROM_D) {
+            cur_k -= 1;
+            cur_e -= 1;
+            gap = 0;
+        } else if (from == FROM_U) {
+            cur_e -= 1;
+            gap = 0;
+        } else {
+            cur_k -= 1;
+            gap += 1;
+            if (gap > max_gap) max_gap = gap;
+        }
+    }
+
+    if (dbg) {
+        if (dbg->bands) memcpy(dbg->bands, bands, sizeof(float) * (size_t)n_bands * W);
+        if (dbg->trace) memcpy(dbg->trace, trace, (size_t)n_bands * W);
+        if (dbg->band_lower_left)
+            memcpy(dbg->band_lower_left, bll, sizeof(abea_event_kmer_pair_t) * (size_t)n_bands);
+        dbg->sum_emission = (flags & ORACLE_QC_FLOAT) ? (double)sum_em_f : sum_em;
+        dbg->path_len = n_out;
+        dbg->max_gap = max_gap;
+    }
+    free(ranks);
+    free(bands);
+    free(trace);
+    free(bll);
+    if (status) return status;
+    if (n_out == 0) return 0; /* reference reads out[-1] here; defined as failure */
+
+    /* reverse in place (align_swi.cpp:1240-1252) */
+    for (int32_t i = 0, j = n_out - 1; i < j; ++i, --j) {
+        abea_aligned_pair_t tmp = out[i];
+        out[i] = out[j];
+        out[j] = tmp;
+    }
+    /* QC (GPU/align_cuda.cl:856-882) */
+    double avg = (flags & ORACLE_QC_FLOAT) ? (double)(sum_em_f / (float)n_aligned)
+                                           : sum_em / n_aligned;
+    int spanned = out[0].ref_pos == 0 && out[n_out - 1].ref_pos == n_kmers - 1;
+    if (avg < MIN_AVG_LOG_EMISSION || !spanned || max_gap > MAX_GAP_THRESHOLD) n_out = 0;
+    return n_out;
+}
+
+/* ---------------- FP64 twin ---------------- */
+static double emission_f64(float x, const abea_model_t *m, abea_scalings_t sc, uint32_t flags) {
+    double gp_mean = (double)sc.scale * m->level_mean + sc.shift;
+    double gp_stdv = m->level_stdv;
+    double gp_log_stdv = (flags & ORACLE_LOG_UNCACHED) ? log((double)m->level_stdv)
+                                                       : (double)m->level_log_stdv;
+    if (flags & ORACLE_VAR_AWARE) {
+        gp_stdv *= sc.var;
+        gp_log_stdv += sc.log_var;
+    }
+    double a = ((double)x - gp_mean) / gp_stdv;
+    return (-0.91893853320467274 - gp_log_stdv) + (-0.5 * a * a);
+}
+
+int32_t oracle_align_f64(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
+                         int32_t seq_len, const abea_event_t *events, int32_t n_events,
+                         const abea_model_t *model, abea_scalings_t sc, uint32_t flags,
+                         double *best_score) {
+    if (best_score) *best_score = -INFINITY;
+    int32_t n_kmers = seq_len - ABEA_KMER_SIZE + 1;
+    if (n_kmers <= 0 || n_events <= 0) return 0;
+    penalties_t pen = make_penalties(n_events, n_kmers);
+    int64_t n_bands = (int64_t)n_events + n_kmers + 2;
+    uint32_t *ranks = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n_kmers);
+    double *bands = (double *)malloc(sizeof(double) * (size_t)n_bands * W);
+    uint8_t *trace = (uint8_t *)calloc((size_t)n_bands * W, 1);
+    abea_event_kmer_pair_t *bll =
+        (abea_event_kmer_pair_t *)malloc(sizeof(abea_event_kmer_pair_t) * (size_t)n_bands);
+    if (!ranks || !bands || !trace || !bll) {
+        free(ranks); free(bands); free(trace); free(bll);
+        return ABEA_ERR_OUT_OF_MEMORY;
+    }
+    for (int32_t k = 0; k < n_kmers; ++k) ranks[k] = oracle_kmer_rank(seq + k);
+    for (int64_t i = 0; i < n_bands * W; ++i) bands[i] = -INFINITY;
+    bll[0].event_idx = HALF_W - 1;
+    bll[0].kmer_idx = -1 - HALF_W;
+    bll[1].event_idx = bll[0].event_idx + 1;
+    bll[1].kmer_idx = bll[0].kmer_idx;
+    BAND(0, -1 - bll[0].kmer_idx) = 0.0;
+    BAND(1, bll[1].event_idx) = pen.lp_trim;
+    TRACE(1, bll[1].event_idx) = FROM_U;
+    for (int64_t b = 2; b < n_bands; ++b) {
+        double ll = BAND(b - 1, 0), ur = BAND(b - 1, W - 1);
+        int right = (ll == -INFINITY && ur == -INFINITY) ? (int)(b & 1) : (ll < ur);
+        abea_event_kmer_pair_t cur = bll[b - 1];
+        if (right) cur.kmer_idx += 1; else cur.event_idx += 1;
+        bll[b] = cur;
+        int trim_offset = -1 - cur.kmer_idx;
+        if (VALID(trim_offset)) {
+            int32_t e = cur.event_idx - trim_offset;
+            if (e >= 0 && e < n_events) {
+                BAND(b, trim_offset) = pen.lp_trim * (e + 1);
+                TRACE(b, trim_offset) = FROM_U;
+            }
+        }
+        int lo = -cur.kmer_idx, t = cur.event_idx - (n_events - 1);
+        if (t > lo) lo = t;
+        if (lo < 0) lo = 0;
+        int hi = n_kmers - cur.kmer_idx;
+        t = cur.event_idx + 1;
+        if (t < hi) hi = t;
+        if (W < hi) hi = W;
+        const abea_event_kmer_pair_t p1 = bll[b - 1], p2 = bll[b - 2];
+        for (int o = lo; o < hi; ++o) {
+            int e = cur.event_idx - o, k = cur.kmer_idx + o;
+            int o_up = p1.event_idx - (e - 1), o_left = (k - 1) - p1.kmer_idx,
+                o_diag = (k - 1) - p2.kmer_idx;
+            double up = VALID(o_up) ? BAND(b - 1, o_up) : -INFINITY;
+            double left = VALID(o_left) ? BAND(b - 1, o_left) : -INFINITY;
+            double diag = VALID(o_diag) ? BAND(b - 2, o_diag) : -INFINITY;
+            double em = emission_f64(events[e].mean, &model[ranks[k]], sc, flags);
+            double s_d = diag + pen.lp_step + em, s_u = up + pen.lp_stay + em,
+                   s_l = left + pen.lp_skip;
+            double best = s_d;
+            uint8_t from = FROM_D;
+            best = s_u > best ? s_u : best;
+            from = best == s_u ? FROM_U : from;
+            best = s_l > best ? s_l : best;
+            from = best == s_l ? FROM_L : from;
+            BAND(b, o) = best;
+            TRACE(b, o) = from;
+        }
+    }
+    double max_score = -INFINITY;
+    int32_t cur_e = 0, cur_k = n_kmers - 1;
+    for (int32_t e = 0; e < n_events; ++e) {
+        int64_t b = (int64_t)e + cur_k + 2;
+        int o = bll[b].event_idx - e;
+        if (VALID(o)) {
+            double s = BAND(b, o) + (n_events - e) * pen.lp_trim;
+            if (s > max_score) {
+                max_score = s;
+                cur_e = e;
+            }
+        }
+    }
+    if (best_score) *best_score = max_score;
+    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0;
+    double sum_em = 0.0;
+    while (cur_k >= 0 && cur_e >= 0) {
+        if (n_out >= out_cap) { status = ABEA_ERR_CAPACITY; break; }
+        out[n_out].ref_pos = cur_k;
+        out[n_out].read_pos = cur_e;
+        n_out++;
+        sum_em += emission_f64(events[cur_e].mean, &model[ranks[cur_k]], sc, flags);
+        int64_t b = (int64_t)cur_e + cur_k + 2;
+        int64_t idx = b * W + (int64_t)(bll[b].event_idx - cur_e);
+        if (idx < 0 || idx >= n_bands * W) { status = ABEA_ERR_UNDEFINED; break; }
+        uint8_t from = trace[idx];
+        if (from == FROM_D) { cur_k--; cur_e--; gap = 0; }
+        else if (from == FROM_U) { cur_e--; gap = 0; }
+        else { cur_k--; gap++; if (gap > max_gap) max_gap = gap; }
+    }
+    free(ranks); free(bands); free(trace); free(bll);
+    if (status) return status;
+    if (n_out == 0) return 0;
+    for (int32_t i = 0, j = n_out - 1; i < j; ++i, --j) {
+        abea_aligned_pair_t tmp = out[i]; out[i] = out[j]; out[j] = tmp;
+    }
+    double avg = sum_em / n_out;
+    int spanned = out[0].ref_pos == 0 && out[n_out - 1].ref_pos == n_kmers - 1;
+    if (avg < MIN_AVG_LOG_EMISSION || !spanned || max_gap > MAX_GAP_THRESHOLD) n_out = 0;
+    return n_out;
+}
+
+/* ---------------- threaded batch (CPU baseline) ---------------- */
+typedef struct {
+    int32_t n_reads;
+    const char *read;
+    const int64_t *read_ptr;
+    const int32_t *read_len;
+    const abea_event_t *event_table;
+    const int64_t *event_ptr;
+    const int32_t *n_events;
+    const abea_scalings_t *scalings;
+    const abea_model_t *model;
+    abea_aligned_pair_t *out_pairs;
+    int32_t *out_n;
+    float *best_scores;
+    uint32_t flags;
+    const int32_t *order;
+    int next;
+    pthread_mutex_t lock;
+} batch_job_t;
+
+static void *batch_worker(void *arg) {
+    batch_job_t *job = (batch_job_t *)arg;
+    for (;;) {
+        pthread_mutex_lock(&job->lock);
+        int slot = job->next++;
+        pthread_mutex_unlock(&job->lock);
+        if (slot >= job->n_reads) break;
+        int32_t i = job->order[slot];
+        oracle_debug_t dbg;
+        memset(&dbg, 0, sizeof(dbg));
+        int32_t ne = job->n_events[i];
+        job->out_n[i] = oracle_align(job->out_pairs + 2 * job->event_ptr[i], 2 * ne,
+                                     job->read + job->read_ptr[i], job->read_len[i],
+                                     job->event_table + job->event_ptr[i], ne, job->model,
+                                     job->scalings[i], job->flags, &dbg);
+        if (job->best_scores) job->best_scores[i] = dbg.best_score;
+    }
+    return NULL;
+}
+
+static const int64_t *g_sort_key;
+static int cmp_desc(const void *a, const void *b) {
+    int64_t ka = g_sort_key[*(const int32_t *)a], kb = g_sort_key[*(const int32_t *)b];
+    if (ka != kb) return ka > kb ? -1 : 1;
+    return *(const int32_t *)a - *(const int32_t *)b;
+}
+
+void oracle_align_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
+                        const int32_t *read_len, const abea_event_t *event_table,
+                        const int64_t *event_ptr, const int32_t *n_events,
+                        const abea_scalings_t *scalings, const abea_model_t *model,
+                        abea_aligned_pair_t *out_pairs, int32_t *out_n, float *best_scores,
+                        uint32_t flags, int n_threads) {
+    if (n_reads <= 0) return;
+    if (n_threads < 1) n_threads = 1;
+    int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)n_reads);
+    int64_t *key = (int64_t *)malloc(sizeof(int64_t) * (size_t)n_reads);
+    for (int32_t i = 0; i < n_reads; ++i) {
+        order[i] = i;
+        key[i] = oracle_n_bands(read_len[i], n_events[i]);
+    }
+    static pthread_mutex_t sort_lock = PTHREAD_MUTEX_INITIALIZER;
+    pthread_mutex_lock(&sort_lock);
+    g_sort_key = key;
+    qsort(order, (size_t)n_reads, sizeof(int32_t), cmp_desc);
+    pthread_mutex_unlock(&sort_lock);
+
+    batch_job_t job = {n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events,
+                       scalings, model, out_pairs, out_n, best_scores, flags, order, 0,
+                       PTHREAD_MUTEX_INITIALIZER};
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)n_threads);
+    int started = 0;
+    for (int t = 0; t < n_threads; ++t)
+        if (pthread_create(&th[t], NULL, batch_worker, &job) == 0) started++;
+        else break;
+    if (started == 0) batch_worker(&job);
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    free(th);
+    free(order);
+    free(key);
+}

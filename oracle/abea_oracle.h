@@ -1,0 +1,85 @@
+/*
+ * abea_oracle.h — CPU oracle for ABEA.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's CPU-side algorithm for f5c's
+ * `align()`: the fill of the single-work-item kernel
+ * (FPGA/code/device/align_swi.cl:184-503) and the best-end / traceback /
+ * quality-check post stage (FPGA/code/host/src/align_swi.cpp:1093-1314, with
+ * the double-precision emission sum of GPU/align_cuda.cl:713-714).  It is the
+ * checker used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg; the product library never links or calls it.
+ *
+ * Pinned against the reference's golden dump (FPGA/code/bins/dump_small, 143
+ * reads, bit-exact AlignedPairs) and against the reference's own SWI code
+ * compiled by oracle/build_ref.sh.  Must be compiled with
+ * -ffp-contract=off (no FMA contraction: the reference has none).
+ */
+#ifndef ABEA_ORACLE_H
+#define ABEA_ORACLE_H
+
+#include "../include/abea.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* flags */
+#define ORACLE_LOG_UNCACHED 0x1 /* gp_log_stdv = (float)log(level_stdv) as align_swi.cl:106-107 */
+#define ORACLE_QC_FLOAT 0x2     /* float sum_emission as align_swi.cpp:1164-1165 */
+#define ORACLE_VAR_AWARE 0x4    /* stdv*var and log_stdv+log_var (not the reference's parity mode) */
+
+/* optional outputs of one alignment; any pointer may be NULL */
+typedef struct {
+    float *bands;                          /* [n_bands*100] scores, reference layout */
+    uint8_t *trace;                        /* [n_bands*100] backpointers */
+    abea_event_kmer_pair_t *band_lower_left; /* [n_bands] */
+    float best_score;                      /* best end score (-inf if none) */
+    int32_t best_event;                    /* event index of the best end */
+    double sum_emission;                   /* QC sum along the path */
+    int32_t path_len;                      /* pairs on the path before QC */
+    int32_t max_gap;
+} oracle_debug_t;
+
+/* One read.  Returns the number of pairs written to out (0 = QC failure), or
+ * ABEA_ERR_CAPACITY / ABEA_ERR_UNDEFINED / ABEA_ERR_INVALID_ARG. */
+int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq, int32_t seq_len,
+                     const abea_event_t *events, int32_t n_events, const abea_model_t *model,
+                     abea_scalings_t scaling, uint32_t flags, oracle_debug_t *dbg);
+
+/* Band count of a read: n_events + n_kmers + 2. */
+int64_t oracle_n_bands(int32_t seq_len, int32_t n_events);
+
+/* Batch in the reference's flattened layout (GPU/align_cuda.c:432-497); reads
+ * are spread over n_threads host threads, longest first.  out_pairs has
+ * capacity 2*n_events[i] at offset 2*event_ptr[i]. */
+void oracle_align_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
+                        const int32_t *read_len, const abea_event_t *event_table,
+                        const int64_t *event_ptr, const int32_t *n_events,
+                        const abea_scalings_t *scalings, const abea_model_t *model,
+                        abea_aligned_pair_t *out_pairs, int32_t *out_n, float *best_scores,
+                        uint32_t flags, int n_threads);
+
+/* FP64 twin: the same recurrence with every score, emission and constant in
+ * double.  Returns the path length after QC like oracle_align; *best_score
+ * receives the double best end score. */
+int32_t oracle_align_f64(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
+                         int32_t seq_len, const abea_event_t *events, int32_t n_events,
+                         const abea_model_t *model, abea_scalings_t scaling, uint32_t flags,
+                         double *best_score);
+
+/* The reference emission, float arithmetic in the reference's order
+ * (GPU/align_cuda.cl:85-110, align_swi.cl:77-111). */
+float oracle_emission(float event_mean, const abea_model_t *m, abea_scalings_t scaling,
+                      uint32_t flags);
+
+/* Rank of the 6-mer starting at s (GPU/align_cuda.cl:22-51). */
+uint32_t oracle_kmer_rank(const char *s);
+
+/* The double-rounded cell sum of the reference, (float)(((double)a + b) + (double)c). */
+float oracle_add3(float a, double b, float c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
