@@ -1,0 +1,292 @@
+"""GB300-native Adaptive Banded Event Alignment (ABEA) — Python host binding.
+
+Mirrors the reference's interface for f5c's align() path:
+  * align(seq, events, model, scalings, sample_rate)  -> AlignedPair array
+      f5c `int32_t align(AlignedPair*, char*, int32_t, event_table, model_t*,
+      scalings_t, float)` (GPU/f5cmisc.h:48-50)
+  * Context.align_batch(batch) -> (pairs, n_pairs)
+      the batch entry align_cuda(core, db) / align_ocl(core, db)
+      (GPU/f5cmisc.h:99-102, GPU/align_cuda.c:391-943), flattened layout of
+      GPU/align_cuda.c:432-497.
+Everything runs in the C-ABI library libabea.so (hand-written sm_103a
+kernels).  There is no CPU path: if the library or a GB300 is missing, the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from . import types
+from .types import (BANDWIDTH, EKPAIR_DTYPE, EVENT_DTYPE, MODEL_DTYPE, PAIR_DTYPE, SCALINGS_DTYPE,
+                    Batch, from_reads, split_pairs)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libabea.so")
+
+MODE_PLAIN = 0
+MODE_BATCHED = 1
+OPT_MODE, OPT_STORE_SCORES, OPT_USE_GRAPH, OPT_LONG_READ_BANDS, OPT_SPIN_LIMIT = range(5)
+
+STATUS = {
+    0: "ok", -1: "invalid argument", -2: "capacity", -3: "out of memory", -4: "CUDA error",
+    -5: "timeout", -6: "no device", -7: "internal", -8: "undefined",
+}
+EXPORTS = [
+    "abea_ctx_create", "abea_ctx_destroy", "abea_ctx_set_option", "abea_ctx_get_option",
+    "abea_last_error", "abea_status_string", "abea_version", "abea_align", "abea_align_cap",
+    "abea_align_batch", "abea_batch_create", "abea_batch_run", "abea_batch_sync",
+    "abea_batch_results", "abea_batch_timing", "abea_batch_destroy", "abea_batch_read_bands",
+    "abea_batch_best_scores", "abea_batch_slow_cells", "abea_host_alloc", "abea_host_free",
+    "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
+    "abea_ctx_flush_l2",
+]
+
+
+class AbeaError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Scalings(C.Structure):
+    _fields_ = [("scale", C.c_float), ("shift", C.c_float), ("var", C.c_float), ("log_var", C.c_float)]
+
+
+class _EventTable(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("start", C.c_size_t), ("end", C.c_size_t), ("event", C.c_void_p)]
+
+
+class Timing(C.Structure):
+    _fields_ = [("pre_ms", C.c_float), ("core_ms", C.c_float), ("post_ms", C.c_float),
+                ("total_ms", C.c_float), ("h2d_ms", C.c_float), ("d2h_ms", C.c_float),
+                ("kernel_launches", C.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+def build(quiet: bool = True) -> str:
+    """Compiles libabea.so in place (nvcc, sm_103a)."""
+    subprocess.run(["make", "-C", HERE, "-j4"], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    """Loads libabea.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise AbeaError(-6, f"{LIB_PATH} is not built; run build()")
+        L = C.CDLL(LIB_PATH)
+        vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+        L.abea_ctx_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int]
+        L.abea_ctx_destroy.argtypes = [vp]
+        L.abea_ctx_destroy.restype = None
+        L.abea_ctx_set_option.argtypes = [vp, C.c_int, i64]
+        L.abea_ctx_get_option.argtypes = [vp, C.c_int, C.POINTER(i64)]
+        L.abea_last_error.restype = C.c_char_p
+        L.abea_version.restype = C.c_char_p
+        L.abea_status_string.restype = C.c_char_p
+        L.abea_status_string.argtypes = [C.c_int]
+        L.abea_align.argtypes = [vp, C.c_char_p, i32, _EventTable, vp, _Scalings, C.c_float]
+        L.abea_align.restype = i32
+        L.abea_align_cap.argtypes = [vp, i32, C.c_char_p, i32, vp, i32, vp, _Scalings]
+        L.abea_align_cap.restype = i32
+        L.abea_align_batch.argtypes = [vp, i32] + [vp] * 10
+        L.abea_batch_create.argtypes = [vp, i32] + [vp] * 8 + [C.POINTER(vp)]
+        L.abea_batch_run.argtypes = [vp, vp]
+        L.abea_batch_sync.argtypes = [vp]
+        L.abea_batch_results.argtypes = [vp, vp, vp, vp]
+        L.abea_batch_timing.argtypes = [vp, vp, C.POINTER(Timing)]
+        L.abea_batch_destroy.argtypes = [vp]
+        L.abea_batch_destroy.restype = None
+        L.abea_batch_read_bands.argtypes = [vp, vp, i32, vp, vp, vp]
+        L.abea_batch_best_scores.argtypes = [vp, vp, vp]
+        L.abea_batch_slow_cells.argtypes = [vp, vp, C.POINTER(i64)]
+        L.abea_host_alloc.argtypes = [C.c_size_t]
+        L.abea_host_alloc.restype = vp
+        L.abea_host_free.argtypes = [vp]
+        L.abea_host_free.restype = None
+        L.abea_ctx_last_timing.argtypes = [vp, C.POINTER(Timing), C.POINTER(i64), C.POINTER(i64)]
+        L.abea_batch_io_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
+        L.abea_ctx_mark.argtypes = [vp, C.c_int]
+        L.abea_ctx_elapsed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
+        L.abea_ctx_flush_l2.argtypes = [vp]
+        _lib = L
+    return _lib
+
+
+def _check(st: int):
+    if st != 0:
+        raise AbeaError(st, lib().abea_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _sc(s) -> _Scalings:
+    return _Scalings(float(s["scale"]), float(s["shift"]), float(s["var"]), float(s["log_var"]))
+
+
+def _batch_arrays(b: Batch):
+    return [np.ascontiguousarray(a) for a in (
+        b.read.astype(np.uint8, copy=False), b.read_ptr.astype(np.int64, copy=False),
+        b.read_len.astype(np.int32, copy=False), np.asarray(b.events, dtype=EVENT_DTYPE),
+        b.event_ptr.astype(np.int64, copy=False), b.n_events.astype(np.int32, copy=False),
+        np.asarray(b.scalings, dtype=SCALINGS_DTYPE), np.asarray(b.model, dtype=MODEL_DTYPE))]
+
+
+class DeviceBatch:
+    """A batch resident in HBM (abea_batch_create)."""
+
+    def __init__(self, ctx: "Context", batch: Batch):
+        self.ctx = ctx
+        self.batch = batch
+        self._arrs = _batch_arrays(batch)
+        h = C.c_void_p()
+        _check(lib().abea_batch_create(ctx.h, batch.n_reads, *[_p(a) for a in self._arrs], C.byref(h)))
+        self.h = h
+
+    def run(self):
+        _check(lib().abea_batch_run(self.ctx.h, self.h))
+
+    def sync(self):
+        _check(lib().abea_batch_sync(self.ctx.h))
+
+    def results(self):
+        pairs = np.zeros(max(self.batch.pair_capacity(), 1), dtype=PAIR_DTYPE)
+        counts = np.zeros(self.batch.n_reads, dtype=np.int32)
+        _check(lib().abea_batch_results(self.ctx.h, self.h, _p(pairs), _p(counts)))
+        return pairs, counts
+
+    def timing(self) -> dict:
+        t = Timing()
+        _check(lib().abea_batch_timing(self.ctx.h, self.h, C.byref(t)))
+        return t.as_dict()
+
+    def best_scores(self):
+        out = np.zeros(self.batch.n_reads, dtype=np.float32)
+        _check(lib().abea_batch_best_scores(self.ctx.h, self.h, _p(out)))
+        return out
+
+    def slow_cells(self) -> int:
+        v = C.c_int64()
+        _check(lib().abea_batch_slow_cells(self.ctx.h, self.h, C.byref(v)))
+        return v.value
+
+    def io_bytes(self):
+        h2d, d2h, cells = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().abea_batch_io_bytes(self.h, C.byref(h2d), C.byref(d2h), C.byref(cells)))
+        return h2d.value, d2h.value, cells.value
+
+    def read_bands(self, i: int, scores: bool = False):
+        """Band matrices of read i in the reference layout: (bands|None, trace, bll)."""
+        b = self.batch
+        nk = int(b.read_len[i]) - 5
+        ne = int(b.n_events[i])
+        if nk <= 0 or ne <= 0:
+            return None, None, None
+        nb = ne + nk + 2
+        bands = np.zeros(nb * BANDWIDTH, dtype=np.float32) if scores else None
+        trace = np.zeros(nb * BANDWIDTH, dtype=np.uint8)
+        bll = np.zeros(nb, dtype=EKPAIR_DTYPE)
+        _check(lib().abea_batch_read_bands(self.ctx.h, self.h, i, _p(bands), _p(trace), _p(bll)))
+        return bands, trace, bll
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().abea_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """One CUDA stream and its buffers (abea_ctx_create)."""
+
+    def __init__(self, device: int = 0, mode: int = MODE_PLAIN, store_scores: bool = False):
+        h = C.c_void_p()
+        _check(lib().abea_ctx_create(C.byref(h), device, mode))
+        self.h = h
+        if store_scores:
+            self.set_option(OPT_STORE_SCORES, 1)
+
+    def set_option(self, opt: int, value: int):
+        _check(lib().abea_ctx_set_option(self.h, opt, int(value)))
+
+    def get_option(self, opt: int) -> int:
+        v = C.c_int64()
+        _check(lib().abea_ctx_get_option(self.h, opt, C.byref(v)))
+        return v.value
+
+    def upload(self, batch: Batch) -> DeviceBatch:
+        return DeviceBatch(self, batch)
+
+    def align_batch(self, batch: Batch, out_pairs=None, out_counts=None):
+        """Host-to-device, align, device-to-host in one call (abea_align_batch)."""
+        arrs = _batch_arrays(batch)
+        pairs = out_pairs if out_pairs is not None else np.zeros(max(batch.pair_capacity(), 1), dtype=PAIR_DTYPE)
+        counts = out_counts if out_counts is not None else np.zeros(batch.n_reads, dtype=np.int32)
+        _check(lib().abea_align_batch(self.h, batch.n_reads, *[_p(a) for a in arrs], _p(pairs), _p(counts)))
+        return pairs, counts
+
+    def last_timing(self):
+        t = Timing()
+        h2d, d2h = C.c_int64(), C.c_int64()
+        _check(lib().abea_ctx_last_timing(self.h, C.byref(t), C.byref(h2d), C.byref(d2h)))
+        return t.as_dict(), h2d.value, d2h.value
+
+    def mark(self, i: int):
+        _check(lib().abea_ctx_mark(self.h, i))
+
+    def elapsed(self, i: int, j: int) -> float:
+        v = C.c_float()
+        _check(lib().abea_ctx_elapsed(self.h, i, j, C.byref(v)))
+        return v.value
+
+    def flush_l2(self):
+        _check(lib().abea_ctx_flush_l2(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().abea_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def align(seq: bytes, events: np.ndarray, model: np.ndarray, scalings, sample_rate: float = 4000.0):
+    """f5c align(): returns the AlignedPair array (empty when QC fails)."""
+    events = np.ascontiguousarray(events, dtype=EVENT_DTYPE)
+    model = np.ascontiguousarray(model, dtype=MODEL_DTYPE)
+    out = np.zeros(max(2 * len(events), 1), dtype=PAIR_DTYPE)
+    et = _EventTable(len(events), 0, len(events), events.ctypes.data)
+    n = lib().abea_align(_p(out), bytes(seq), len(seq), et, _p(model), _sc(scalings), float(sample_rate))
+    if n < 0:
+        raise AbeaError(n, lib().abea_last_error().decode())
+    return out[:n]
+
+
+def version() -> str:
+    return lib().abea_version().decode()
+
+
+__all__ = ["align", "Context", "DeviceBatch", "Batch", "from_reads", "split_pairs", "build", "lib",
+           "AbeaError", "MODE_PLAIN", "MODE_BATCHED", "types", "EXPORTS", "version"]

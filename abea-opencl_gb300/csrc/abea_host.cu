@@ -1,0 +1,810 @@
+// abea_host.cu — host orchestration and the C ABI (include/abea.h).
+//
+// Mirrors the reference's batch entry align_ocl(core, db) (GPU/align_cuda.c:391-943):
+// flatten -> size buffers -> host-to-device copies -> pre/core/post -> device-to-host
+// copies, but with one device slab per batch (reused across calls), all copies
+// and kernels queued on one CUDA stream per context, per-stage CUDA-event timing,
+// and status codes instead of printing and continuing.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "abea_internal.h"
+#include "abea_launch.h"
+
+using namespace abea;
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+static abea_status_t fail(abea_status_t st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return st;
+}
+
+#define CUDA_TRY(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t err__ = (call);                                                      \
+        if (err__ != cudaSuccess) {                                                      \
+            abea_status_t st__ = err__ == cudaErrorMemoryAllocation ? ABEA_ERR_OUT_OF_MEMORY \
+                                                                    : ABEA_ERR_CUDA;     \
+            return fail(st__, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(err__), \
+                        __FILE__, __LINE__);                                             \
+        }                                                                                \
+    } while (0)
+
+extern "C" const char* abea_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char* abea_status_string(abea_status_t s) {
+    switch (s) {
+    case ABEA_OK: return "ok";
+    case ABEA_ERR_INVALID_ARG: return "invalid argument";
+    case ABEA_ERR_CAPACITY: return "alignment longer than its output slot";
+    case ABEA_ERR_OUT_OF_MEMORY: return "out of memory";
+    case ABEA_ERR_CUDA: return "CUDA error";
+    case ABEA_ERR_TIMEOUT: return "device wait timed out";
+    case ABEA_ERR_NO_DEVICE: return "no usable CUDA device";
+    case ABEA_ERR_INTERNAL: return "internal consistency check failed";
+    case ABEA_ERR_UNDEFINED: return "reference behaviour undefined for this read";
+    }
+    return "unknown status";
+}
+
+extern "C" const char* abea_version(void) { return "abea-gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------- objects
+struct DevSlab {
+    void* base = nullptr;
+    size_t bytes = 0;
+};
+
+struct abea_batch {
+    abea_ctx* ctx = nullptr;
+    int32_t n_reads = 0;
+    std::vector<ReadDesc> reads;
+    std::vector<int32_t> order;  // longest first
+    int32_t n_wide = 0;          // leading reads of `order` run on the wide shape
+    // sizes
+    int64_t seq_bytes = 0, n_events_total = 0, ev_pad_total = 0, km_pad_total = 0,
+            band_pad_total = 0, pair_cap = 0, band_cells = 0;
+    // device pointers (sub-ranges of the slab)
+    DevSlab slab;
+    ReadDesc* d_reads = nullptr;
+    char* d_seq = nullptr;
+    abea_event_t* d_ev = nullptr;
+    abea_model_t* d_model = nullptr;
+    float *d_ev_mean = nullptr, *d_km_gm = nullptr, *d_km_sd = nullptr, *d_km_k1 = nullptr,
+          *d_last_col = nullptr;
+    uint8_t* d_trace = nullptr;
+    float* d_scores = nullptr;
+    int32_t* d_band_k0 = nullptr;
+    abea_aligned_pair_t* d_pairs = nullptr;
+    int32_t* d_n_pairs = nullptr;
+    float* d_best = nullptr;
+    int32_t* d_status = nullptr;
+    unsigned long long* d_slow = nullptr;
+    int32_t* d_order = nullptr;
+    int32_t* d_queue = nullptr;
+    bool scores_kept = false;
+    bool ran = false;
+    abea_timing_t timing{};
+    cudaGraphExec_t graph = nullptr;
+    int graph_mode = -1;
+};
+
+struct abea_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    abea_mode_t mode = ABEA_MODE_PLAIN;
+    int64_t store_scores = 0;
+    int64_t use_graph = 1;
+    int64_t long_read_bands = 0;
+    int64_t spin_limit = 1 << 22;
+    int sm_count = 0;
+    cudaEvent_t ev[8] = {};
+    cudaEvent_t marker[16] = {};
+    void* flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    abea_batch* scratch = nullptr;  // reused by abea_align_batch / abea_align
+};
+
+// ---------------------------------------------------------------- context
+extern "C" abea_status_t abea_ctx_create(abea_ctx_t** out, int device, abea_mode_t mode) {
+    if (!out) return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_create: null output pointer");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0)
+        return fail(ABEA_ERR_NO_DEVICE, "abea_ctx_create: no CUDA device");
+    if (device < 0 || device >= n)
+        return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_create: device %d out of range", device);
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    if (prop.major * 10 + prop.minor != 103)
+        return fail(ABEA_ERR_NO_DEVICE,
+                    "abea_ctx_create: device %d is sm_%d%d; this library is built for sm_103a only",
+                    device, prop.major, prop.minor);
+    abea_ctx* c = new (std::nothrow) abea_ctx();
+    if (!c) return fail(ABEA_ERR_OUT_OF_MEMORY, "abea_ctx_create: host allocation failed");
+    c->device = device;
+    c->mode = mode;
+    c->sm_count = prop.multiProcessorCount;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->ev[i]);
+    for (int i = 0; i < 16 && e == cudaSuccess; ++i) e = cudaEventCreate(&c->marker[i]);
+    if (e != cudaSuccess) {
+        abea_ctx_destroy(c);
+        return fail(ABEA_ERR_CUDA, "abea_ctx_create: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return ABEA_OK;
+}
+
+static void free_batch_device(abea_batch* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    if (b->slab.base) cudaFree(b->slab.base);
+    b->slab = DevSlab{};
+}
+
+extern "C" void abea_batch_destroy(abea_batch_t* b) {
+    if (!b) return;
+    free_batch_device(b);
+    delete b;
+}
+
+extern "C" void abea_ctx_destroy(abea_ctx_t* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->scratch) abea_batch_destroy(c->scratch);
+    for (int i = 0; i < 8; ++i)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i < 16; ++i)
+        if (c->marker[i]) cudaEventDestroy(c->marker[i]);
+    if (c->flush_buf) cudaFree(c->flush_buf);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" abea_status_t abea_ctx_set_option(abea_ctx_t* c, abea_option_t opt, int64_t v) {
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_set_option: null context");
+    switch (opt) {
+    case ABEA_OPT_MODE:
+        if (v != ABEA_MODE_PLAIN && v != ABEA_MODE_BATCHED)
+            return fail(ABEA_ERR_INVALID_ARG, "unknown mode %lld", (long long)v);
+        c->mode = (abea_mode_t)v;
+        return ABEA_OK;
+    case ABEA_OPT_STORE_SCORES: c->store_scores = v != 0; return ABEA_OK;
+    case ABEA_OPT_USE_GRAPH: c->use_graph = v != 0; return ABEA_OK;
+    case ABEA_OPT_LONG_READ_BANDS:
+        if (v < 0) return fail(ABEA_ERR_INVALID_ARG, "negative band threshold");
+        c->long_read_bands = v;
+        return ABEA_OK;
+    case ABEA_OPT_SPIN_LIMIT:
+        if (v <= 0) return fail(ABEA_ERR_INVALID_ARG, "spin limit must be positive");
+        c->spin_limit = v;
+        return ABEA_OK;
+    }
+    return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
+}
+
+extern "C" abea_status_t abea_ctx_get_option(abea_ctx_t* c, abea_option_t opt, int64_t* v) {
+    if (!c || !v) return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_get_option: null argument");
+    switch (opt) {
+    case ABEA_OPT_MODE: *v = c->mode; return ABEA_OK;
+    case ABEA_OPT_STORE_SCORES: *v = c->store_scores; return ABEA_OK;
+    case ABEA_OPT_USE_GRAPH: *v = c->use_graph; return ABEA_OK;
+    case ABEA_OPT_LONG_READ_BANDS: *v = c->long_read_bands; return ABEA_OK;
+    case ABEA_OPT_SPIN_LIMIT: *v = c->spin_limit; return ABEA_OK;
+    }
+    return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
+}
+
+extern "C" void* abea_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    return p;
+}
+extern "C" void abea_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+// ---------------------------------------------------------------- planning
+struct Penalties {
+    double lp_skip, lp_stay, lp_step, lp_trim;
+};
+
+// Transition log-probabilities of a read, computed on the host with the C
+// library's log/exp exactly as the reference does (align_swi.cl:233-250).
+static Penalties penalties(int32_t n_events, int32_t n_kmers) {
+    Penalties p;
+    double events_per_kmer = (double)n_events / n_kmers;
+    double p_stay = 1 - (1 / (events_per_kmer + 1));
+    p.lp_skip = log(1e-10);
+    p.lp_stay = log(p_stay);
+    p.lp_step = log(1.0 - exp(p.lp_skip) - exp(p.lp_stay));
+    p.lp_trim = log(0.01);
+    return p;
+}
+
+static void split(double v, float& h, float& l) {
+    h = (float)v;
+    l = (float)(v - (double)h);
+}
+
+static float pow2_floor(float x) {
+    int e;
+    frexpf(x, &e);  // x = m * 2^e, m in [0.5,1)
+    return ldexpf(1.0f, e - 1);
+}
+
+static GlobalConsts global_consts(int var_aware) {
+    GlobalConsts g;
+    g.lp_skip = log(1e-10);
+    g.lp_trim = log(0.01);
+    split(g.lp_skip, g.skip_h, g.skip_l);
+    g.trim_f = (float)g.lp_trim;
+    g.var_aware = var_aware;
+    return g;
+}
+
+struct HostInputs {
+    int32_t n_reads;
+    const char* read;
+    const int64_t* read_ptr;
+    const int32_t* read_len;
+    const abea_event_t* event_table;
+    const int64_t* event_ptr;
+    const int32_t* n_events;
+    const abea_scalings_t* scalings;
+    const abea_model_t* model;
+};
+
+static abea_status_t validate(const HostInputs& in) {
+    if (in.n_reads < 0) return fail(ABEA_ERR_INVALID_ARG, "n_reads < 0");
+    if (in.n_reads == 0) return ABEA_OK;
+    if (!in.read || !in.read_ptr || !in.read_len || !in.event_ptr || !in.n_events ||
+        !in.scalings || !in.model)
+        return fail(ABEA_ERR_INVALID_ARG, "null input array");
+    for (int32_t i = 0; i < in.n_reads; ++i) {
+        if (in.read_len[i] < 0 || in.n_events[i] < 0 || in.read_ptr[i] < 0 || in.event_ptr[i] < 0)
+            return fail(ABEA_ERR_INVALID_ARG, "read %d: negative length or offset", i);
+        if (in.n_events[i] > 0 && !in.event_table)
+            return fail(ABEA_ERR_INVALID_ARG, "null event table");
+        if ((int64_t)in.n_events[i] > (1ll << 30) || (int64_t)in.read_len[i] > (1ll << 30))
+            return fail(ABEA_ERR_INVALID_ARG, "read %d too long", i);
+    }
+    return ABEA_OK;
+}
+
+// Offsets and per-read constants of a batch.
+static abea_status_t plan(abea_batch* b, const HostInputs& in) {
+    b->n_reads = in.n_reads;
+    b->reads.assign((size_t)in.n_reads, ReadDesc{});
+    int64_t seq_end = 0, ev_end = 0, km = 0, ev = 0, bands = 0, cells = 0;
+    for (int32_t i = 0; i < in.n_reads; ++i) {
+        ReadDesc& r = b->reads[(size_t)i];
+        int32_t len = in.read_len[i], ne = in.n_events[i];
+        int32_t nk = len - ABEA_KMER_SIZE + 1;
+        r.seq_off = in.read_ptr[i];
+        r.ev_src = in.event_ptr[i];
+        r.out_off = 2 * in.event_ptr[i];
+        r.n_events = ne;
+        r.n_kmers = nk;
+        r.out_cap = 2 * ne;
+        r.scale = in.scalings[i].scale;
+        r.shift = in.scalings[i].shift;
+        r.var = in.scalings[i].var;
+        r.log_var = in.scalings[i].log_var;
+        seq_end = std::max(seq_end, in.read_ptr[i] + (int64_t)len);
+        ev_end = std::max(ev_end, in.event_ptr[i] + (int64_t)ne);
+        r.skip = (nk <= 0 || ne <= 0) ? 1 : 0;
+        if (r.skip) {
+            r.n_bands = 0;
+            r.ev_off = ev;
+            r.km_off = km;
+            r.band_off = bands;
+            continue;
+        }
+        r.n_bands = ne + nk + 2;
+        Penalties p = penalties(ne, nk);
+        r.lp_step = p.lp_step;
+        r.lp_stay = p.lp_stay;
+        split(p.lp_step, r.step_h, r.step_l);
+        split(p.lp_stay, r.stay_h, r.stay_l);
+        r.b_max = std::max(fabsf(r.step_h), fabsf(r.stay_h));
+        r.em_floor = pow2_floor(r.b_max);
+        r.ev_off = ev;
+        r.km_off = km;
+        r.band_off = bands;
+        ev += round_up(ne, kChunk);
+        km += round_up(nk, kChunk);
+        bands += round_up(r.n_bands, 4);
+        cells += (int64_t)r.n_bands * kBand;
+    }
+    b->seq_bytes = seq_end;
+    b->n_events_total = ev_end;
+    b->ev_pad_total = ev;
+    b->km_pad_total = km;
+    b->band_pad_total = bands;
+    b->pair_cap = 2 * ev_end;
+    b->band_cells = cells;
+    // longest first; ties by index
+    b->order.resize((size_t)in.n_reads);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int32_t x, int32_t y) {
+        return b->reads[(size_t)x].n_bands > b->reads[(size_t)y].n_bands;
+    });
+    return ABEA_OK;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Carves the device slab; grows it when needed.
+static abea_status_t ensure_device(abea_batch* b, bool scores) {
+    size_t n = (size_t)std::max(b->n_reads, 1);
+    size_t sizes[20] = {
+        sizeof(ReadDesc) * n,                                   // reads
+        (size_t)std::max<int64_t>(b->seq_bytes, 1),             // seq
+        sizeof(abea_event_t) * (size_t)std::max<int64_t>(b->n_events_total, 1),
+        sizeof(abea_model_t) * ABEA_NUM_KMER,
+        sizeof(float) * (size_t)std::max<int64_t>(b->ev_pad_total, 16),  // ev_mean
+        sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // gm
+        sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // sd
+        sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // k1
+        sizeof(float) * (size_t)std::max<int64_t>(b->ev_pad_total, 16),  // last_col
+        (size_t)kSlots * (size_t)std::max<int64_t>(b->band_pad_total, 4), // trace
+        scores ? sizeof(float) * kSlots * (size_t)std::max<int64_t>(b->band_pad_total, 4) : 0,
+        sizeof(int32_t) * (size_t)std::max<int64_t>(b->band_pad_total, 4),  // band_k0
+        sizeof(abea_aligned_pair_t) * (size_t)std::max<int64_t>(b->pair_cap, 1),
+        sizeof(int32_t) * n,   // n_pairs
+        sizeof(float) * n,     // best
+        sizeof(int32_t) * n,   // status
+        sizeof(unsigned long long) * 4,  // slow counter
+        sizeof(int32_t) * n,   // order
+        sizeof(int32_t) * 8,   // queue counters
+        0};
+    size_t total = 0;
+    for (size_t s : sizes) total += align256(s);
+    if (total > b->slab.bytes) {
+        free_batch_device(b);
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, total);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ABEA_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed: %s", total,
+                        cudaGetErrorString(e));
+        }
+        b->slab.base = p;
+        b->slab.bytes = total;
+    }
+    char* p = (char*)b->slab.base;
+    void* ptrs[20];
+    for (int i = 0; i < 19; ++i) {
+        ptrs[i] = sizes[i] ? (void*)p : nullptr;
+        p += align256(sizes[i]);
+    }
+    b->d_reads = (ReadDesc*)ptrs[0];
+    b->d_seq = (char*)ptrs[1];
+    b->d_ev = (abea_event_t*)ptrs[2];
+    b->d_model = (abea_model_t*)ptrs[3];
+    b->d_ev_mean = (float*)ptrs[4];
+    b->d_km_gm = (float*)ptrs[5];
+    b->d_km_sd = (float*)ptrs[6];
+    b->d_km_k1 = (float*)ptrs[7];
+    b->d_last_col = (float*)ptrs[8];
+    b->d_trace = (uint8_t*)ptrs[9];
+    b->d_scores = (float*)ptrs[10];
+    b->d_band_k0 = (int32_t*)ptrs[11];
+    b->d_pairs = (abea_aligned_pair_t*)ptrs[12];
+    b->d_n_pairs = (int32_t*)ptrs[13];
+    b->d_best = (float*)ptrs[14];
+    b->d_status = (int32_t*)ptrs[15];
+    b->d_slow = (unsigned long long*)ptrs[16];
+    b->d_order = (int32_t*)ptrs[17];
+    b->d_queue = (int32_t*)ptrs[18];
+    b->scores_kept = scores;
+    return ABEA_OK;
+}
+
+static abea_status_t upload(abea_batch* b, const HostInputs& in, cudaStream_t st) {
+    if (b->n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaMemcpyAsync(b->d_reads, b->reads.data(), sizeof(ReadDesc) * b->reads.size(),
+                             cudaMemcpyHostToDevice, st));
+    if (b->seq_bytes > 0)
+        CUDA_TRY(cudaMemcpyAsync(b->d_seq, in.read, (size_t)b->seq_bytes, cudaMemcpyHostToDevice, st));
+    if (b->n_events_total > 0)
+        CUDA_TRY(cudaMemcpyAsync(b->d_ev, in.event_table, sizeof(abea_event_t) * (size_t)b->n_events_total,
+                                 cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(b->d_model, in.model, sizeof(abea_model_t) * ABEA_NUM_KMER,
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(b->d_order, b->order.data(), sizeof(int32_t) * b->order.size(),
+                             cudaMemcpyHostToDevice, st));
+    return ABEA_OK;
+}
+
+static int64_t h2d_bytes(const abea_batch* b) {
+    return (int64_t)(sizeof(ReadDesc) * b->reads.size()) + b->seq_bytes +
+           (int64_t)sizeof(abea_event_t) * b->n_events_total + (int64_t)sizeof(abea_model_t) * ABEA_NUM_KMER +
+           (int64_t)sizeof(int32_t) * (int64_t)b->order.size();
+}
+
+static int64_t d2h_bytes(const abea_batch* b) {
+    return (int64_t)sizeof(abea_aligned_pair_t) * b->pair_cap + (int64_t)sizeof(int32_t) * b->n_reads;
+}
+
+// Queues pre, core and post for a batch on the context's stream.
+static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches) {
+    LaunchArgs la;
+    la.reads = b->d_reads;
+    la.n_reads = b->n_reads;
+    la.g = global_consts(0);
+    la.seq = b->d_seq;
+    la.ev_in = b->d_ev;
+    la.model = b->d_model;
+    la.ev_mean = b->d_ev_mean;
+    la.km_gm = b->d_km_gm;
+    la.km_sd = b->d_km_sd;
+    la.km_k1 = b->d_km_k1;
+    la.last_col = b->d_last_col;
+    la.trace = b->d_trace;
+    la.scores = b->scores_kept ? b->d_scores : nullptr;
+    la.band_k0 = b->d_band_k0;
+    la.pairs = b->d_pairs;
+    la.n_pairs = b->d_n_pairs;
+    la.best = b->d_best;
+    la.status = b->d_status;
+    la.slow = b->d_slow;
+    la.order = b->d_order;
+    la.queue = b->d_queue;
+    la.n_wide = b->n_wide;
+    la.sm_count = c->sm_count;
+    la.spin_limit = (int32_t)std::min<int64_t>(c->spin_limit, 0x7fffffff);
+    la.stream = c->stream;
+    la.ev_pre = c->ev[1];
+    la.ev_core = c->ev[2];
+    cudaError_t e = c->mode == ABEA_MODE_BATCHED ? launch_batched(la, launches)
+                                                 : launch_plain(la, launches);
+    if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+    return ABEA_OK;
+}
+
+static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
+    CUDA_TRY(cudaSetDevice(c->device));
+    b->timing = abea_timing_t{};
+    if (b->n_reads == 0) {
+        b->ran = true;
+        return ABEA_OK;
+    }
+    // wide shape for the longest reads in the batched form
+    b->n_wide = 0;
+    if (c->mode == ABEA_MODE_BATCHED) b->n_wide = choose_wide_reads(b->reads, b->order, c->sm_count, c->long_read_bands);
+    CUDA_TRY(cudaMemsetAsync(b->d_slow, 0, sizeof(unsigned long long), c->stream));
+    CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int32_t) * 8, c->stream));
+    CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
+    int launches = 0;
+    abea_status_t st = launch_all(c, b, &launches);
+    if (st) return st;
+    CUDA_TRY(cudaEventRecord(c->ev[3], c->stream));
+    b->timing.kernel_launches = launches;
+    b->ran = true;
+    return ABEA_OK;
+}
+
+static abea_status_t collect_timing(abea_ctx* c, abea_batch* b) {
+    if (b->n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaEventSynchronize(c->ev[3]));
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, c->ev[0], c->ev[1]));
+    b->timing.pre_ms = t;
+    CUDA_TRY(cudaEventElapsedTime(&t, c->ev[1], c->ev[2]));
+    b->timing.core_ms = t;
+    CUDA_TRY(cudaEventElapsedTime(&t, c->ev[2], c->ev[3]));
+    b->timing.post_ms = t;
+    CUDA_TRY(cudaEventElapsedTime(&t, c->ev[0], c->ev[3]));
+    b->timing.total_ms = t;
+    return ABEA_OK;
+}
+
+static abea_status_t download(abea_ctx* c, abea_batch* b, abea_aligned_pair_t* pairs, int32_t* n_pairs) {
+    if (b->n_reads == 0) return ABEA_OK;
+    if (pairs && b->pair_cap > 0)
+        CUDA_TRY(cudaMemcpyAsync(pairs, b->d_pairs, sizeof(abea_aligned_pair_t) * (size_t)b->pair_cap,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    if (n_pairs)
+        CUDA_TRY(cudaMemcpyAsync(n_pairs, b->d_n_pairs, sizeof(int32_t) * (size_t)b->n_reads,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    return ABEA_OK;
+}
+
+static abea_status_t check_status(abea_ctx* c, abea_batch* b) {
+    if (b->n_reads == 0) return ABEA_OK;
+    std::vector<int32_t> st((size_t)b->n_reads);
+    CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_status, sizeof(int32_t) * st.size(), cudaMemcpyDeviceToHost,
+                             c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < st.size(); ++i)
+        if (st[i] != 0)
+            return fail((abea_status_t)st[i], "read %zu: %s", i, abea_status_string((abea_status_t)st[i]));
+    return ABEA_OK;
+}
+
+// ---------------------------------------------------------------- batch API
+static HostInputs inputs(int32_t n, const char* read, const int64_t* read_ptr, const int32_t* read_len,
+                         const abea_event_t* ev, const int64_t* event_ptr, const int32_t* n_events,
+                         const abea_scalings_t* sc, const abea_model_t* model) {
+    HostInputs in{n, read, read_ptr, read_len, ev, event_ptr, n_events, sc, model};
+    return in;
+}
+
+extern "C" abea_status_t abea_batch_create(abea_ctx_t* c, int32_t n_reads, const char* read,
+                                           const int64_t* read_ptr, const int32_t* read_len,
+                                           const abea_event_t* event_table, const int64_t* event_ptr,
+                                           const int32_t* n_events, const abea_scalings_t* scalings,
+                                           const abea_model_t* model, abea_batch_t** out) {
+    if (!c || !out) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_create: null argument");
+    *out = nullptr;
+    HostInputs in = inputs(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model);
+    abea_status_t st = validate(in);
+    if (st) return st;
+    CUDA_TRY(cudaSetDevice(c->device));
+    abea_batch* b = new (std::nothrow) abea_batch();
+    if (!b) return fail(ABEA_ERR_OUT_OF_MEMORY, "host allocation failed");
+    b->ctx = c;
+    if ((st = plan(b, in)) || (st = ensure_device(b, c->store_scores != 0)) || (st = upload(b, in, c->stream))) {
+        abea_batch_destroy(b);
+        return st;
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        abea_batch_destroy(b);
+        return fail(ABEA_ERR_CUDA, "upload failed: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_run(abea_ctx_t* c, abea_batch_t* b) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_run: null argument");
+    if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
+    return run_batch(c, b);
+}
+
+extern "C" abea_status_t abea_batch_sync(abea_ctx_t* c) {
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_sync: null context");
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_results(abea_ctx_t* c, abea_batch_t* b, abea_aligned_pair_t* pairs,
+                                            int32_t* n_pairs) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_results: null argument");
+    if (!b->ran) return fail(ABEA_ERR_INVALID_ARG, "batch has not been run");
+    abea_status_t st = download(c, b, pairs, n_pairs);
+    if (st) return st;
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return check_status(c, b);
+}
+
+extern "C" abea_status_t abea_batch_timing(abea_ctx_t* c, abea_batch_t* b, abea_timing_t* t) {
+    if (!c || !b || !t) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_timing: null argument");
+    abea_status_t st = collect_timing(c, b);
+    if (st) return st;
+    *t = b->timing;
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_best_scores(abea_ctx_t* c, abea_batch_t* b, float* best) {
+    if (!c || !b || !best) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_best_scores: null argument");
+    if (b->n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaMemcpyAsync(best, b->d_best, sizeof(float) * (size_t)b->n_reads, cudaMemcpyDeviceToHost,
+                             c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_slow_cells(abea_ctx_t* c, abea_batch_t* b, int64_t* count) {
+    if (!c || !b || !count) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_slow_cells: null argument");
+    unsigned long long v = 0;
+    if (b->n_reads) {
+        CUDA_TRY(cudaMemcpyAsync(&v, b->d_slow, sizeof(v), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    *count = (int64_t)v;
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_read_bands(abea_ctx_t* c, abea_batch_t* b, int32_t ri, float* bands,
+                                               uint8_t* trace, abea_event_kmer_pair_t* bll) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_read_bands: null argument");
+    if (ri < 0 || ri >= b->n_reads) return fail(ABEA_ERR_INVALID_ARG, "read index out of range");
+    if (bands && !b->scores_kept)
+        return fail(ABEA_ERR_INVALID_ARG, "scores were not kept (ABEA_OPT_STORE_SCORES)");
+    const ReadDesc& r = b->reads[(size_t)ri];
+    if (r.skip) return ABEA_OK;
+    int64_t nb = r.n_bands, nbp = round_up(nb, 4);
+    std::vector<uint8_t> tr((size_t)(nbp * kSlots));
+    std::vector<int32_t> k0((size_t)nbp);
+    std::vector<float> sc;
+    CUDA_TRY(cudaMemcpyAsync(tr.data(), b->d_trace + r.band_off * kSlots, tr.size(), cudaMemcpyDeviceToHost,
+                             c->stream));
+    CUDA_TRY(cudaMemcpyAsync(k0.data(), b->d_band_k0 + r.band_off, sizeof(int32_t) * k0.size(),
+                             cudaMemcpyDeviceToHost, c->stream));
+    if (bands) {
+        sc.resize((size_t)(nbp * kSlots));
+        CUDA_TRY(cudaMemcpyAsync(sc.data(), b->d_scores + r.band_off * kSlots, sizeof(float) * sc.size(),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    // slot layout -> reference layout: offset o of band b is k-mer k0+o, slot (k0+o)&127
+    for (int64_t bi = 0; bi < nb; ++bi) {
+        int32_t kk = k0[(size_t)bi];
+        if (bll) {
+            bll[bi].kmer_idx = kk;
+            bll[bi].event_idx = (int32_t)(bi - 2 - kk);
+        }
+        for (int o = 0; o < kBand; ++o) {
+            int slot = (kk + o) & 127;
+            if (trace) trace[bi * kBand + o] = tr[(size_t)trace_index(bi, slot)];
+            if (bands) bands[bi * kBand + o] = sc[(size_t)(bi * kSlots + slot)];
+        }
+    }
+    return ABEA_OK;
+}
+
+// ---------------------------------------------------------------- one-call batch
+static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_aligned_pair_t* pairs,
+                                      int32_t* n_pairs) {
+    abea_status_t st = validate(in);
+    if (st) return st;
+    CUDA_TRY(cudaSetDevice(c->device));
+    if (!c->scratch) {
+        c->scratch = new (std::nothrow) abea_batch();
+        if (!c->scratch) return fail(ABEA_ERR_OUT_OF_MEMORY, "host allocation failed");
+        c->scratch->ctx = c;
+    }
+    abea_batch* b = c->scratch;
+    if ((st = plan(b, in)) || (st = ensure_device(b, c->store_scores != 0))) return st;
+    CUDA_TRY(cudaEventRecord(c->ev[4], c->stream));
+    if ((st = upload(b, in, c->stream))) return st;
+    CUDA_TRY(cudaEventRecord(c->ev[5], c->stream));
+    if ((st = run_batch(c, b))) return st;
+    CUDA_TRY(cudaEventRecord(c->ev[6], c->stream));
+    if ((st = download(c, b, pairs, n_pairs))) return st;
+    CUDA_TRY(cudaEventRecord(c->ev[7], c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if ((st = collect_timing(c, b))) return st;
+    float t = 0;
+    CUDA_TRY(cudaEventElapsedTime(&t, c->ev[4], c->ev[5]));
+    b->timing.h2d_ms = t;
+    CUDA_TRY(cudaEventElapsedTime(&t, c->ev[6], c->ev[7]));
+    b->timing.d2h_ms = t;
+    return check_status(c, b);
+}
+
+extern "C" abea_status_t abea_align_batch(abea_ctx_t* c, int32_t n_reads, const char* read,
+                                          const int64_t* read_ptr, const int32_t* read_len,
+                                          const abea_event_t* event_table, const int64_t* event_ptr,
+                                          const int32_t* n_events, const abea_scalings_t* scalings,
+                                          const abea_model_t* model, abea_aligned_pair_t* event_align_pairs,
+                                          int32_t* n_event_align_pairs) {
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_align_batch: null context");
+    if (n_reads > 0 && (!event_align_pairs || !n_event_align_pairs))
+        return fail(ABEA_ERR_INVALID_ARG, "abea_align_batch: null output");
+    HostInputs in = inputs(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model);
+    return align_batch_impl(c, in, event_align_pairs, n_event_align_pairs);
+}
+
+extern "C" abea_status_t abea_ctx_last_timing(abea_ctx_t* c, abea_timing_t* t, int64_t* h2d, int64_t* d2h) {
+    if (!c || !t) return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_last_timing: null argument");
+    if (!c->scratch) return fail(ABEA_ERR_INVALID_ARG, "no batch has run on this context");
+    *t = c->scratch->timing;
+    if (h2d) *h2d = h2d_bytes(c->scratch);
+    if (d2h) *d2h = d2h_bytes(c->scratch);
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_io_bytes(abea_batch_t* b, int64_t* h2d, int64_t* d2h, int64_t* band_cells) {
+    if (!b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_io_bytes: null batch");
+    if (h2d) *h2d = h2d_bytes(b);
+    if (d2h) *d2h = d2h_bytes(b);
+    if (band_cells) *band_cells = b->band_cells;
+    return ABEA_OK;
+}
+
+// ---------------------------------------------------------------- f5c align()
+// One context per calling thread: f5c calls align() from its worker threads
+// (GPU/f5c.h:57-59), so each thread queues on its own stream.
+struct ThreadCtx {
+    abea_ctx* ctx = nullptr;
+    ~ThreadCtx() {
+        if (ctx) abea_ctx_destroy(ctx);
+    }
+};
+static thread_local ThreadCtx t_ctx;
+
+extern "C" int32_t abea_align_cap(abea_aligned_pair_t* out_2, int32_t out_capacity, const char* sequence,
+                                  int32_t sequence_len, const abea_event_t* events, int32_t n_events,
+                                  const abea_model_t* models, abea_scalings_t scaling) {
+    if (!out_2 || !sequence || !models || out_capacity < 0 || sequence_len < 0 || n_events < 0 ||
+        (n_events > 0 && !events))
+        return fail(ABEA_ERR_INVALID_ARG, "abea_align: invalid argument");
+    if (!t_ctx.ctx) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        abea_status_t st = abea_ctx_create(&t_ctx.ctx, dev, ABEA_MODE_PLAIN);
+        if (st) return st;
+    }
+    abea_ctx* c = t_ctx.ctx;
+    int64_t read_ptr = 0, event_ptr = 0;
+    int32_t npairs = 0;
+    // the batch output has room for 2*n_events pairs; stage it when the caller's
+    // slot is smaller
+    std::vector<abea_aligned_pair_t> tmp((size_t)std::max(2 * n_events, 1));
+    HostInputs in = inputs(1, sequence, &read_ptr, &sequence_len, events, &event_ptr, &n_events, &scaling, models);
+    abea_status_t st = align_batch_impl(c, in, tmp.data(), &npairs);
+    if (st) return st;
+    if (npairs < 0) return npairs;
+    if (npairs > out_capacity) return fail(ABEA_ERR_CAPACITY, "abea_align: %d pairs exceed capacity %d", npairs, out_capacity);
+    memcpy(out_2, tmp.data(), sizeof(abea_aligned_pair_t) * (size_t)npairs);
+    return npairs;
+}
+
+extern "C" int32_t abea_align(abea_aligned_pair_t* out_2, char* sequence, int32_t sequence_len,
+                              abea_event_table_t events, abea_model_t* models, abea_scalings_t scaling,
+                              float sample_rate) {
+    (void)sample_rate;  // unused by the algorithm, as in the reference
+    if (events.n > (size_t)0x3fffffff) return fail(ABEA_ERR_INVALID_ARG, "abea_align: too many events");
+    int32_t ne = (int32_t)events.n;
+    return abea_align_cap(out_2, 2 * ne, sequence, sequence_len, events.event, ne, models, scaling);
+}
+
+// f5c's own symbol: a weak alias, so that an f5c build that drops its CPU
+// align.c links this library in its place while a build that keeps it wins.
+extern "C" int32_t align(abea_aligned_pair_t* out_2, char* sequence, int32_t sequence_len,
+                         abea_event_table_t events, abea_model_t* models, abea_scalings_t scaling,
+                         float sample_rate) __attribute__((weak, alias("abea_align")));
+
+// ---------------------------------------------------------------- timing helpers
+extern "C" abea_status_t abea_ctx_mark(abea_ctx_t* c, int i) {
+    if (!c || i < 0 || i >= 16) return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_mark: bad argument");
+    CUDA_TRY(cudaEventRecord(c->marker[i], c->stream));
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_ctx_elapsed(abea_ctx_t* c, int i, int j, float* ms) {
+    if (!c || !ms || i < 0 || i >= 16 || j < 0 || j >= 16)
+        return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_elapsed: bad argument");
+    CUDA_TRY(cudaEventSynchronize(c->marker[j]));
+    CUDA_TRY(cudaEventElapsedTime(ms, c->marker[i], c->marker[j]));
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_ctx_flush_l2(abea_ctx_t* c) {
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_ctx_flush_l2: null context");
+    CUDA_TRY(cudaSetDevice(c->device));
+    if (!c->flush_buf) {
+        int l2 = 0;
+        CUDA_TRY(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device));
+        size_t bytes = std::max<size_t>((size_t)l2 * 2, (size_t)256 << 20);
+        CUDA_TRY(cudaMalloc(&c->flush_buf, bytes));
+        c->flush_bytes = bytes;
+    }
+    static int flip = 0;
+    CUDA_TRY(cudaMemsetAsync(c->flush_buf, (flip++) & 0xff, c->flush_bytes, c->stream));
+    return ABEA_OK;
+}

@@ -1,0 +1,398 @@
+#!/usr/bin/env python3
+"""ABEA benchmark: band-cells/s (and reads/s) of the GB300 library on the f5c
+batch workload, against the reference's CPU align() on the host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one pass of pre/core/post over the whole synthetic batch (1.3 Mbases,
+lognormal read lengths, median 3 kb, clipped 500 b - 20 kb), inputs resident in
+HBM, L2 flushed before every timed step.  `e2e` is the same metric through
+abea_align_batch with pinned host buffers (host->device and device->host copies
+inside the timed region).  Under torchrun every rank aligns its own shard of the
+reads (longest-processing-time partition by band cells, no collective on the data
+path; weak scaling) and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+BYTES_PER_CELL = 5  # 4 B score + 1 B backpointer per band cell (the reference's layout)
+
+
+def load_package():
+    pkg_dir = os.path.join(ROOT, "abea-opencl_gb300")
+    spec = importlib.util.spec_from_file_location(
+        "abea_gb300", os.path.join(pkg_dir, "__init__.py"), submodule_search_locations=[pkg_dir])
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["abea_gb300"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+WORKLOADS = {
+    "f5c_batch": "reads totalling 1.3 Mbases, lognormal lengths (median 3 kb, sigma 0.6) clipped to 500 b-20 kb",
+    "uneven": "1.3 Mbases: 80% of reads U(200 b, 5 kb), 20% U(20 kb, 100 kb)",
+    "small": "64 reads, U(1 kb, 3 kb)",
+}
+
+
+# ---------------------------------------------------------------- distributed helpers
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def shard_reads(n_bands: np.ndarray, world: int, rank: int) -> np.ndarray:
+    """Longest-processing-time partition of reads over ranks by band cells."""
+    order = np.argsort(-n_bands, kind="stable")
+    load = np.zeros(world, dtype=np.int64)
+    owner = np.zeros(len(n_bands), dtype=np.int64)
+    for i in order:
+        r = int(np.argmin(load))
+        owner[i] = r
+        load[r] += int(n_bands[i])
+    return np.nonzero(owner == rank)[0]
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in self.rows for j in range(4) if r[5 + j].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def measured_traffic_per_cell():
+    """DRAM bytes per band cell of the core kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "core_dram_bytes.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_band_cell"]), d
+    except (OSError, KeyError, ValueError):
+        return None, None
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_align(batch, threads: int):
+    from oracle import oracle
+    t0 = time.perf_counter()
+    oracle.align_batch(batch, threads=threads)
+    return time.perf_counter() - t0
+
+
+def reference_arm(args, dist):
+    """The reference's CPU align() path on the host cores (the oracle port of
+    align_swi.cl + align_swi.cpp; the reference's own code when it compiled here)."""
+    if dist.rank != 0:
+        return 0
+    pkg = load_package()
+    from abea_gb300 import synth
+    from oracle import oracle
+    oracle.build()
+    batch = synth.make_batch(args.workload, seed=args.seed)
+    threads = os.cpu_count() or 1
+    kind = "port"
+    for _ in range(args.warmup if args.warmup < 2 else 1):
+        cpu_align(batch, threads)
+    times = [cpu_align(batch, threads) for _ in range(args.steps)]
+    t = sum(times) / len(times)
+    cells = batch.band_cells()
+    v = cells / t
+    line = {
+        "impl": "reference", "metric": "ABEA band-cells/s (f5c align, adaptive band 100)",
+        "value": v, "unit": "band-cells/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 scores, f64 transition adds", "data": "synthetic",
+        "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload),
+                   "reads": batch.n_reads, "band_cells": cells, "seed": args.seed},
+        "reads_per_s": batch.n_reads / t,
+        "cpu_baseline": {"value": v, "unit": "band-cells/s", "cores": threads, "kind": kind,
+                         "sample": f"the whole {args.workload} batch per step"},
+        "e2e": {"value": v, "unit": "band-cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU side
+def time_device(pkg, ctx, dev, steps: int, warmup: int):
+    for _ in range(warmup):
+        dev.run()
+        dev.sync()
+    per_step, core = [], []
+    for _ in range(steps):
+        ctx.flush_l2()
+        ctx.mark(0)
+        dev.run()
+        ctx.mark(1)
+        per_step.append(ctx.elapsed(0, 1))
+        core.append(dev.timing()["core_ms"])
+    return per_step, core, dev.timing()
+
+
+def time_e2e(pkg, ctx, batch, steps: int, warmup: int):
+    import ctypes as C
+    L = pkg.lib()
+    # pinned host copies of the inputs and outputs
+    arrs = pkg._batch_arrays(batch)
+    pinned = []
+    for a in arrs:
+        p = L.abea_host_alloc(max(a.nbytes, 1))
+        if not p:
+            raise MemoryError("pinned allocation failed")
+        C.memmove(p, a.ctypes.data, a.nbytes)
+        pinned.append(p)
+    cap = max(batch.pair_capacity(), 1)
+    out_p = L.abea_host_alloc(cap * 8)
+    out_n = L.abea_host_alloc(max(batch.n_reads, 1) * 4)
+    try:
+        def call():
+            st = L.abea_align_batch(ctx.h, batch.n_reads, *pinned, out_p, out_n)
+            if st:
+                raise pkg.AbeaError(st, L.abea_last_error().decode())
+        for _ in range(warmup):
+            call()
+        ts = []
+        for _ in range(steps):
+            ctx.flush_l2()
+            ctx.mark(0)
+            ctx.elapsed(0, 0)
+            t0 = time.perf_counter()
+            call()
+            ts.append(time.perf_counter() - t0)
+        timing, h2d, d2h = ctx.last_timing()
+        return ts, timing, h2d, d2h
+    finally:
+        for p in pinned + [out_p, out_n]:
+            L.abea_host_free(p)
+
+
+def run_mode(pkg, batch, mode, device, steps, warmup):
+    ctx = pkg.Context(device, mode)
+    dev = ctx.upload(batch)
+    per_step, core, timing = time_device(pkg, ctx, dev, steps, warmup)
+    res = dict(per_step=per_step, core=core, timing=timing, slow=dev.slow_cells())
+    dev.close()
+    ctx.close()
+    return res
+
+
+def ours(args, dist):
+    pkg = load_package()
+    from abea_gb300 import synth
+    device = dist.local_rank
+    full = synth.make_batch(args.workload, seed=args.seed)
+    shard = shard_reads(full.n_bands(), dist.world, dist.rank) if dist.world > 1 else np.arange(full.n_reads)
+    batch = full.subset(shard) if dist.world > 1 else full
+    cells = batch.band_cells()
+    mode = pkg.MODE_BATCHED if args.mode == "batched" else pkg.MODE_PLAIN
+
+    ctx = pkg.Context(device, mode)
+    dev = ctx.upload(batch)
+    launches_per_step = None
+    for _ in range(args.warmup):
+        dev.run()
+        dev.sync()
+    dist.barrier()
+    clocks = ClockSampler(device)
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    per_step, core = [], []
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        ctx.mark(0)
+        dev.run()
+        ctx.mark(1)
+        per_step.append(ctx.elapsed(0, 1))
+        tm = dev.timing()
+        core.append(tm["core_ms"])
+        launches_per_step = tm["kernel_launches"]
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    slow = dev.slow_cells()
+    dev.close()
+    local_ms = sum(per_step)
+    dist.barrier()
+    max_ms = dist.max(local_ms)
+    total_cells = dist.sum(float(cells))
+    total_reads = dist.sum(float(batch.n_reads))
+    ms_per_step = max_ms / args.steps
+    value = total_cells / (ms_per_step / 1e3)
+
+    # end to end through abea_align_batch (pinned host buffers)
+    e2e_ts, e2e_timing, h2d, d2h = time_e2e(pkg, ctx, batch, args.steps, 1)
+    e2e_s = dist.max(sum(e2e_ts)) / args.steps
+    ctx.close()
+
+    if dist.rank != 0:
+        return 0
+    out = {
+        "metric": "ABEA band-cells/s (f5c align, adaptive band 100)",
+        "value": value, "unit": "band-cells/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 scores, f64 transition adds (emulated exactly)",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload),
+                   "reads": int(total_reads), "band_cells": int(total_cells), "seed": args.seed,
+                   "mode": args.mode, "parallelism": f"reads sharded over {dist.world} GPU(s)",
+                   "l2": "flushed (write of 2x L2) before every timed step"},
+        "reads_per_s": total_reads / (ms_per_step / 1e3),
+        "gpu_launches": int(launches_per_step or 0) * args.steps,
+        "wall_s_timed_region": wall,
+        "slow_cells_fp64": slow,
+        "clocks": clk,
+        "e2e": {"value": total_cells / e2e_s, "unit": "band-cells/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                "stage_ms": {k: round(v, 4) for k, v in e2e_timing.items() if k.endswith("_ms")}},
+    }
+    # roofline of the dominant kernel (core), algorithmic bytes = 5 B per band cell
+    peak, peak_kind = measured_peak_hbm()
+    core_ms = statistics.mean(core)
+    achieved = BYTES_PER_CELL * cells / (core_ms / 1e3) / 1e9
+    tpc, tinfo = measured_traffic_per_cell()
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                       "frac": achieved / peak, "peak_kind": f"{peak_kind} (hbm_gbs)",
+                       "traffic": (tpc * cells) if tpc else None,
+                       "kernel": "abea_core (fill)", "core_ms": core_ms,
+                       "algorithmic_bytes": BYTES_PER_CELL * cells}
+    if tinfo:
+        out["roofline"]["traffic_source"] = tinfo.get("source")
+    if args.compare and dist.world == 1:
+        other = "plain" if args.mode == "batched" else "batched"
+        om = pkg.MODE_PLAIN if other == "plain" else pkg.MODE_BATCHED
+        r = run_mode(pkg, batch, om, device, max(2, args.steps // 2), 1)
+        ms = statistics.mean(r["per_step"])
+        out[other] = {"value": cells / (ms / 1e3), "ms_per_step": ms, "core_ms": statistics.mean(r["core"])}
+        # the uneven (heavy-tail) 1.3 Mbase batch, both forms
+        ub = synth.make_batch("uneven", seed=args.seed)
+        un = {}
+        for name, m in (("batched", pkg.MODE_BATCHED), ("plain", pkg.MODE_PLAIN)):
+            r = run_mode(pkg, ub, m, device, 2, 1)
+            ms = statistics.mean(r["per_step"])
+            un[name] = {"value": ub.band_cells() / (ms / 1e3), "ms_per_step": ms}
+        un["batched_over_plain"] = un["batched"]["value"] / un["plain"]["value"]
+        un["workload"] = WORKLOADS["uneven"]
+        out["uneven"] = un
+    if args.cpu and dist.world == 1:
+        threads = os.cpu_count() or 1
+        t = cpu_align(batch, threads)
+        out["cpu_baseline"] = {"value": cells / t, "unit": "band-cells/s", "cores": threads, "kind": "port",
+                               "sample": f"the whole {args.workload} batch, once"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="f5c_batch")
+    ap.add_argument("--mode", choices=["batched", "plain"], default="batched")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-compare", dest="compare", action="store_false")
+    ap.add_argument("--no-cpu", dest="cpu", action="store_false")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        rc = reference_arm(args, dist) if args.impl == "reference" else ours(args, dist)
+    finally:
+        dist.close()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

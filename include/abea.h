@@ -196,6 +196,29 @@ abea_status_t abea_batch_best_scores(abea_ctx_t *ctx, abea_batch_t *batch, float
  * FP64 slow path during the last run (diagnostic). */
 abea_status_t abea_batch_slow_cells(abea_ctx_t *ctx, abea_batch_t *batch, int64_t *count);
 
+/* Pinned host memory for fast host<->device copies (cudaHostAlloc). */
+void *abea_host_alloc(size_t bytes);
+void abea_host_free(void *ptr);
+
+/* Timing and copy volume of the last abea_align_batch / abea_align call on a
+ * context: stage times, and the host->device / device->host bytes moved. */
+abea_status_t abea_ctx_last_timing(abea_ctx_t *ctx, abea_timing_t *timing, int64_t *h2d_bytes,
+                                   int64_t *d2h_bytes);
+
+/* Copy volume of a batch and its band-cell count (sum of n_bands*100). */
+abea_status_t abea_batch_io_bytes(abea_batch_t *batch, int64_t *h2d_bytes, int64_t *d2h_bytes,
+                                  int64_t *band_cells);
+
+/* Timing markers on the context's stream (CUDA events), for callers that time
+ * several runs as one region: abea_ctx_mark(ctx, i) records marker i (0..15);
+ * abea_ctx_elapsed(ctx, i, j, &ms) waits for marker j and returns j - i. */
+abea_status_t abea_ctx_mark(abea_ctx_t *ctx, int marker);
+abea_status_t abea_ctx_elapsed(abea_ctx_t *ctx, int from_marker, int to_marker, float *ms);
+
+/* Evicts the GPU's L2 cache by writing a buffer larger than it on the
+ * context's stream (benchmark hygiene between timed runs). */
+abea_status_t abea_ctx_flush_l2(abea_ctx_t *ctx);
+
 #ifdef __cplusplus
 }
 #endif

@@ -224,17 +224,20 @@ int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
     }
 
     /* ---- traceback (align_swi.cpp:1178-1236) ---- */
-    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0;
+    /* A path longer than the output slot makes the reference write past it
+     * (into the next read's slot in a batch); the walk continues without
+     * writing so that the QC verdict is still the reference's, and such a read
+     * is reported as ABEA_ERR_CAPACITY only when it passes QC. */
+    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0, last_k = cur_k;
     double sum_em = 0.0;
     float sum_em_f = 0.0f;
     double n_aligned = 0.0;
     while (cur_k >= 0 && cur_e >= 0) {
-        if (n_out >= out_cap) {
-            status = ABEA_ERR_CAPACITY;
-            break;
+        if (n_out < out_cap) {
+            out[n_out].ref_pos = cur_k;
+            out[n_out].read_pos = cur_e;
         }
-        out[n_out].ref_pos = cur_k;
-        out[n_out].read_pos = cur_e;
+        last_k = cur_k;
         n_out++;
         float em = oracle_emission(events[cur_e].mean, &model[ranks[cur_k]], sc, flags);
         sum_em += (double)em;
@@ -280,17 +283,19 @@ int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
     if (status) return status;
     if (n_out == 0) return 0; /* reference reads out[-1] here; defined as failure */
 
+    /* QC (GPU/align_cuda.cl:856-882).  After the reversal out[0] is the last
+     * cell walked and out[n-1] the first, (n_kmers-1, best end). */
+    double avg = (flags & ORACLE_QC_FLOAT) ? (double)(sum_em_f / (float)n_aligned)
+                                           : sum_em / n_aligned;
+    int spanned = last_k == 0;
+    if (avg < MIN_AVG_LOG_EMISSION || !spanned || max_gap > MAX_GAP_THRESHOLD) return 0;
+    if (n_out > out_cap) return ABEA_ERR_CAPACITY;
     /* reverse in place (align_swi.cpp:1240-1252) */
     for (int32_t i = 0, j = n_out - 1; i < j; ++i, --j) {
         abea_aligned_pair_t tmp = out[i];
         out[i] = out[j];
         out[j] = tmp;
     }
-    /* QC (GPU/align_cuda.cl:856-882) */
-    double avg = (flags & ORACLE_QC_FLOAT) ? (double)(sum_em_f / (float)n_aligned)
-                                           : sum_em / n_aligned;
-    int spanned = out[0].ref_pos == 0 && out[n_out - 1].ref_pos == n_kmers - 1;
-    if (avg < MIN_AVG_LOG_EMISSION || !spanned || max_gap > MAX_GAP_THRESHOLD) n_out = 0;
     return n_out;
 }
 
@@ -391,12 +396,14 @@ int32_t oracle_align_f64(abea_aligned_pair_t *out, int32_t out_cap, const char *
         }
     }
     if (best_score) *best_score = max_score;
-    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0;
+    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0, last_k = cur_k;
     double sum_em = 0.0;
     while (cur_k >= 0 && cur_e >= 0) {
-        if (n_out >= out_cap) { status = ABEA_ERR_CAPACITY; break; }
-        out[n_out].ref_pos = cur_k;
-        out[n_out].read_pos = cur_e;
+        if (n_out < out_cap) {
+            out[n_out].ref_pos = cur_k;
+            out[n_out].read_pos = cur_e;
+        }
+        last_k = cur_k;
         n_out++;
         sum_em += emission_f64(events[cur_e].mean, &model[ranks[cur_k]], sc, flags);
         int64_t b = (int64_t)cur_e + cur_k + 2;
@@ -410,12 +417,12 @@ int32_t oracle_align_f64(abea_aligned_pair_t *out, int32_t out_cap, const char *
     free(ranks); free(bands); free(trace); free(bll);
     if (status) return status;
     if (n_out == 0) return 0;
+    double avg = sum_em / n_out;
+    if (avg < MIN_AVG_LOG_EMISSION || last_k != 0 || max_gap > MAX_GAP_THRESHOLD) return 0;
+    if (n_out > out_cap) return ABEA_ERR_CAPACITY;
     for (int32_t i = 0, j = n_out - 1; i < j; ++i, --j) {
         abea_aligned_pair_t tmp = out[i]; out[i] = out[j]; out[j] = tmp;
     }
-    double avg = sum_em / n_out;
-    int spanned = out[0].ref_pos == 0 && out[n_out - 1].ref_pos == n_kmers - 1;
-    if (avg < MIN_AVG_LOG_EMISSION || !spanned || max_gap > MAX_GAP_THRESHOLD) n_out = 0;
     return n_out;
 }
 

@@ -1,0 +1,62 @@
+"""The C-ABI library: it builds, loads and exports every declared entry point
+(no device calls: this file runs without a GPU)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT, abea
+
+HEADER = os.path.join(ROOT, "include", "abea.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(abea_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    if not os.path.exists(abea.LIB_PATH):
+        abea.build()
+    return abea.LIB_PATH
+
+
+def test_header_declares_the_f5c_entry():
+    names = declared_functions()
+    for n in ("abea_align", "abea_align_batch", "abea_batch_create", "abea_batch_run",
+              "abea_ctx_create", "abea_ctx_destroy", "abea_last_error"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    out = subprocess.run(["nm", "-D", "--defined-only", libpath], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(line.split()[-1] for line in out.splitlines() if line.strip())
+    missing = [n for n in declared_functions() if n not in exported]
+    assert missing == []
+    # f5c's own symbol, as a weak alias of abea_align
+    assert "align" in exported
+
+
+def test_library_loads_with_ctypes(libpath):
+    L = C.CDLL(libpath)
+    for n in declared_functions():
+        assert hasattr(L, n)
+    assert set(abea.EXPORTS) <= set(declared_functions())
+
+
+def test_no_torch_or_oracle_in_library(libpath):
+    out = subprocess.run(["nm", "-D", "--undefined-only", libpath], capture_output=True, text=True,
+                         check=True).stdout
+    assert "oracle_" not in out and "torch" not in out
+
+
+def test_status_strings_without_device(libpath):
+    L = abea.lib()
+    assert L.abea_status_string(-2).decode().startswith("alignment longer")
+    assert L.abea_version().decode().startswith("abea-gb300")

@@ -1,0 +1,162 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle and the
+reference's golden vectors.  Bit-exact for AlignedPairs, counts, band scores,
+backpointers and band placements (integer/index results and the reference's
+own float rounding)."""
+import numpy as np
+import pytest
+
+from conftest import abea
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import os
+    if not os.path.exists(abea.LIB_PATH):
+        abea.build()
+    return abea.lib()
+
+
+def run(batch, mode=abea.MODE_PLAIN, scores=False):
+    ctx = abea.Context(0, mode, store_scores=scores)
+    pairs, counts = ctx.align_batch(batch)
+    return ctx, pairs, counts
+
+
+def oracle_batch(oracle_mod, batch):
+    return oracle_mod.align_batch(batch, threads=os.cpu_count())
+
+
+import os  # noqa: E402
+
+
+def assert_same_alignments(batch, pairs, counts, opairs, ocounts):
+    assert np.array_equal(counts, ocounts)
+    got = abea.split_pairs(batch, pairs, counts)
+    exp = abea.split_pairs(batch, opairs, ocounts)
+    for i in range(batch.n_reads):
+        assert np.array_equal(got[i], exp[i]), f"read {i}"
+
+
+@pytest.mark.parametrize("mode", [abea.MODE_PLAIN, abea.MODE_BATCHED])
+def test_dump_subset_matches_f5c(lib, dump_subset, mode):
+    batch, golden = dump_subset
+    _, pairs, counts = run(batch, mode)
+    got = abea.split_pairs(batch, pairs, counts)
+    for i, g in enumerate(golden):
+        assert counts[i] == len(g)
+        assert np.array_equal(got[i], g)
+
+
+@pytest.mark.parametrize("mode", [abea.MODE_PLAIN, abea.MODE_BATCHED])
+def test_edge_cases_match_reference(lib, oracle_mod, ref_synthetic, mode):
+    batch, names, counts, pairs, bands = ref_synthetic
+    ctx = abea.Context(0, mode, store_scores=True)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
+    assert np.array_equal(gc, counts)
+    for i, name in enumerate(names):
+        if name not in bands:
+            continue
+        b, t, bll = dev.read_bands(i, scores=True)
+        rb, rt, rbll = bands[name]
+        assert np.array_equal(b.view(np.uint32), rb.view(np.uint32)), name
+        assert np.array_equal(t, rt), name
+        assert np.array_equal(bll.view(np.int32).reshape(-1, 2), rbll), name
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_small_workload_bit_exact(lib, oracle_mod, seed):
+    from abea_gb300 import synth
+    batch = synth.make_batch("small", seed=seed)
+    ctx = abea.Context(0, abea.MODE_PLAIN, store_scores=True)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    op, oc, obest = oracle_batch(oracle_mod, batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
+    assert np.array_equal(dev.best_scores().view(np.uint32), obest.view(np.uint32))
+    for i in (0, 7, 63):
+        b, t, bll = dev.read_bands(i, scores=True)
+        _, _, info = oracle_mod.align(batch.sequence(i), batch.read_events(i), batch.model,
+                                      batch.scalings[i], want_bands=True)
+        assert np.array_equal(b.view(np.uint32), info["bands"].view(np.uint32))
+        assert np.array_equal(t, info["trace"])
+        assert np.array_equal(bll, info["bll"])
+
+
+def test_low_skip_reads_pass_qc_bit_exact(lib, oracle_mod):
+    """Reads that pass QC (1% skipped k-mers), so the pair lists are non-empty."""
+    from abea_gb300 import synth
+    rng = np.random.default_rng(3)
+    model = synth.make_model(rng)
+    seqs, evs, scs = [], [], []
+    for L in rng.integers(500, 4000, 24):
+        s, e = synth.make_read(rng, model, L, 1.0, 2.0, 1.2, skip_p=0.01)
+        seqs.append(s.tobytes())
+        evs.append(e)
+        scs.append((1.0, 2.0, 1.2, np.log(1.2)))
+    batch = abea.from_reads(seqs, evs, np.array(scs, dtype=abea.types.SCALINGS_DTYPE), model)
+    _, gp, gc = run(batch)
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    assert (oc > 0).sum() >= 20
+    assert_same_alignments(batch, gp, gc, op, oc)
+
+
+def test_single_read_drop_in(lib, oracle_mod, dump_subset):
+    """abea_align(): f5c's align() signature, one read at a time."""
+    batch, golden = dump_subset
+    for i in range(batch.n_reads):
+        p = abea.align(batch.sequence(i), batch.read_events(i), batch.model, batch.scalings[i], 4000.0)
+        assert np.array_equal(p, golden[i])
+
+
+def test_fp64_fallback_cells_stay_exact(lib, oracle_mod):
+    """A pore model with level_stdv near 0.4 makes emissions tiny, which defeats
+    the FP32 exactness proof and sends many cells down the FP64 path."""
+    from abea_gb300 import synth
+    rng = np.random.default_rng(17)
+    model = synth.make_model(rng)
+    model["level_stdv"] = rng.uniform(0.38, 0.42, len(model)).astype(np.float32)
+    model["level_log_stdv"] = np.log(model["level_stdv"].astype(np.float64)).astype(np.float32)
+    seqs, evs, scs = [], [], []
+    for L in (300, 800, 1500):
+        s, e = synth.make_read(rng, model, L, 1.0, 0.0, 0.3, skip_p=0.01)
+        seqs.append(s.tobytes())
+        evs.append(e)
+        scs.append((1.0, 0.0, 1.0, 0.0))
+    batch = abea.from_reads(seqs, evs, np.array(scs, dtype=abea.types.SCALINGS_DTYPE), model)
+    ctx = abea.Context(0, abea.MODE_PLAIN)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
+    assert dev.slow_cells() > 1000
+
+
+def test_degenerate_reads(lib, oracle_mod):
+    """Reads shorter than a k-mer, reads without events, non-ACGT bases."""
+    from abea_gb300 import synth
+    rng = np.random.default_rng(23)
+    model = synth.make_model(rng)
+    ev = np.zeros(10, dtype=abea.types.EVENT_DTYPE)
+    ev["mean"] = rng.uniform(60, 130, 10)
+    seqs = [b"ACG", b"ACGTACGTAC", b"NNNNNNNNNNNN", b"ACGTAC"]
+    evs = [ev, ev[:0], ev, ev[:1]]
+    scs = np.array([(1.0, 0.0, 1.0, 0.0)] * 4, dtype=abea.types.SCALINGS_DTYPE)
+    batch = abea.from_reads(seqs, evs, scs, model)
+    _, gp, gc = run(batch)
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
+
+
+def test_empty_batch(lib):
+    from abea_gb300 import synth
+    b = synth.make_batch("small", seed=1).subset([])
+    _, pairs, counts = run(b)
+    assert len(counts) == 0
