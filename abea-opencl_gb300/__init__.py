@@ -42,7 +42,7 @@ EXPORTS = [
     "abea_batch_results", "abea_batch_timing", "abea_batch_destroy", "abea_batch_read_bands",
     "abea_batch_best_scores", "abea_batch_slow_cells", "abea_host_alloc", "abea_host_free",
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
-    "abea_ctx_flush_l2",
+    "abea_ctx_flush_l2", "abea_selftest_arith",
 ]
 
 
@@ -120,6 +120,7 @@ def lib():
         L.abea_ctx_mark.argtypes = [vp, C.c_int]
         L.abea_ctx_elapsed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.abea_ctx_flush_l2.argtypes = [vp]
+        L.abea_selftest_arith.argtypes = [i64, C.c_uint64, vp]
         _lib = L
     return _lib
 
@@ -284,9 +285,18 @@ def align(seq: bytes, events: np.ndarray, model: np.ndarray, scalings, sample_ra
     return out[:n]
 
 
+def selftest_arith(cases: int = 1 << 26, seed: int = 1) -> dict:
+    """Device self-test of the exact FP32 arithmetic (see include/abea.h)."""
+    out = np.zeros(5, dtype=np.int64)
+    _check(lib().abea_selftest_arith(int(cases), int(seed), _p(out)))
+    return dict(div_wrong=int(out[0]), div_declined=int(out[1]), sum_wrong=int(out[2]),
+                sum_declined=int(out[3]), cases=int(out[4]))
+
+
 def version() -> str:
     return lib().abea_version().decode()
 
 
 __all__ = ["align", "Context", "DeviceBatch", "Batch", "from_reads", "split_pairs", "build", "lib",
-           "AbeaError", "MODE_PLAIN", "MODE_BATCHED", "types", "EXPORTS", "version"]
+           "AbeaError", "MODE_PLAIN", "MODE_BATCHED", "types", "EXPORTS", "version",
+           "selftest_arith"]

@@ -87,8 +87,8 @@ struct abea_batch {
     char* d_seq = nullptr;
     abea_event_t* d_ev = nullptr;
     abea_model_t* d_model = nullptr;
-    float *d_ev_mean = nullptr, *d_km_gm = nullptr, *d_km_sd = nullptr, *d_km_k1 = nullptr,
-          *d_last_col = nullptr;
+    float *d_ev_mean = nullptr, *d_km_gm = nullptr, *d_km_sd = nullptr, *d_km_rsd = nullptr,
+          *d_km_k1 = nullptr, *d_last_col = nullptr;
     uint8_t* d_trace = nullptr;
     float* d_scores = nullptr;
     int32_t* d_band_k0 = nullptr;
@@ -292,8 +292,22 @@ static abea_status_t validate(const HostInputs& in) {
 }
 
 // Offsets and per-read constants of a batch.
+// 1 when log_inv_sqrt_2pi - log(stdv) <= 0 for every k-mer of the model (with
+// the read's log_var in var-aware mode): then every emission and every score of
+// the read is <= 0, which the kernels' fast tier relies on.
+static int model_nonpos(const abea_model_t* model, float log_var, int var_aware) {
+    for (int k = 0; k < ABEA_NUM_KMER; ++k) {
+        volatile float lsd = model[k].level_log_stdv;
+        if (var_aware) lsd = lsd + log_var;
+        volatile float k1 = -0.918938f - lsd;
+        if (!(k1 <= 0.0f)) return 0;
+    }
+    return 1;
+}
+
 static abea_status_t plan(abea_batch* b, const HostInputs& in) {
     b->n_reads = in.n_reads;
+    const int nonpos = in.n_reads > 0 ? model_nonpos(in.model, 0.0f, 0) : 1;
     b->reads.assign((size_t)in.n_reads, ReadDesc{});
     int64_t seq_end = 0, ev_end = 0, km = 0, ev = 0, bands = 0, cells = 0;
     for (int32_t i = 0; i < in.n_reads; ++i) {
@@ -328,6 +342,7 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in) {
         split(p.lp_stay, r.stay_h, r.stay_l);
         r.b_max = std::max(fabsf(r.step_h), fabsf(r.stay_h));
         r.em_floor = pow2_floor(r.b_max);
+        r.nonpos = nonpos;
         r.ev_off = ev;
         r.km_off = km;
         r.band_off = bands;
@@ -357,7 +372,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Carves the device slab; grows it when needed.
 static abea_status_t ensure_device(abea_batch* b, bool scores) {
     size_t n = (size_t)std::max(b->n_reads, 1);
-    size_t sizes[20] = {
+    size_t sizes[21] = {
         sizeof(ReadDesc) * n,                                   // reads
         (size_t)std::max<int64_t>(b->seq_bytes, 1),             // seq
         sizeof(abea_event_t) * (size_t)std::max<int64_t>(b->n_events_total, 1),
@@ -367,6 +382,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // sd
         sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // k1
         sizeof(float) * (size_t)std::max<int64_t>(b->ev_pad_total, 16),  // last_col
+        sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // rsd
         (size_t)kSlots * (size_t)std::max<int64_t>(b->band_pad_total, 4), // trace
         scores ? sizeof(float) * kSlots * (size_t)std::max<int64_t>(b->band_pad_total, 4) : 0,
         sizeof(int32_t) * (size_t)std::max<int64_t>(b->band_pad_total, 4),  // band_k0
@@ -378,8 +394,9 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         sizeof(int32_t) * n,   // order
         sizeof(int32_t) * 8,   // queue counters
         0};
+    const int n_bufs = 20;
     size_t total = 0;
-    for (size_t s : sizes) total += align256(s);
+    for (int i = 0; i < n_bufs; ++i) total += align256(sizes[i]);
     if (total > b->slab.bytes) {
         free_batch_device(b);
         void* p = nullptr;
@@ -393,8 +410,8 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         b->slab.bytes = total;
     }
     char* p = (char*)b->slab.base;
-    void* ptrs[20];
-    for (int i = 0; i < 19; ++i) {
+    void* ptrs[21];
+    for (int i = 0; i < n_bufs; ++i) {
         ptrs[i] = sizes[i] ? (void*)p : nullptr;
         p += align256(sizes[i]);
     }
@@ -407,16 +424,17 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
     b->d_km_sd = (float*)ptrs[6];
     b->d_km_k1 = (float*)ptrs[7];
     b->d_last_col = (float*)ptrs[8];
-    b->d_trace = (uint8_t*)ptrs[9];
-    b->d_scores = (float*)ptrs[10];
-    b->d_band_k0 = (int32_t*)ptrs[11];
-    b->d_pairs = (abea_aligned_pair_t*)ptrs[12];
-    b->d_n_pairs = (int32_t*)ptrs[13];
-    b->d_best = (float*)ptrs[14];
-    b->d_status = (int32_t*)ptrs[15];
-    b->d_slow = (unsigned long long*)ptrs[16];
-    b->d_order = (int32_t*)ptrs[17];
-    b->d_queue = (int32_t*)ptrs[18];
+    b->d_km_rsd = (float*)ptrs[9];
+    b->d_trace = (uint8_t*)ptrs[10];
+    b->d_scores = (float*)ptrs[11];
+    b->d_band_k0 = (int32_t*)ptrs[12];
+    b->d_pairs = (abea_aligned_pair_t*)ptrs[13];
+    b->d_n_pairs = (int32_t*)ptrs[14];
+    b->d_best = (float*)ptrs[15];
+    b->d_status = (int32_t*)ptrs[16];
+    b->d_slow = (unsigned long long*)ptrs[17];
+    b->d_order = (int32_t*)ptrs[18];
+    b->d_queue = (int32_t*)ptrs[19];
     b->scores_kept = scores;
     return ABEA_OK;
 }
@@ -447,38 +465,40 @@ static int64_t d2h_bytes(const abea_batch* b) {
     return (int64_t)sizeof(abea_aligned_pair_t) * b->pair_cap + (int64_t)sizeof(int32_t) * b->n_reads;
 }
 
+// Reads of the batched form that run on the wide (4-warp) shape: the longest
+// reads whose band count exceeds what one warp would carry if the whole batch
+// were spread evenly over the resident warps (their warp-shape fill would
+// outlast the rest of the batch), at most one per resident block.
+static int choose_wide_reads(const abea_batch* b, int sm_count, int64_t threshold, bool scores) {
+    const int blocks = batched_blocks_per_sm(scores) * sm_count;
+    int64_t total = 0;
+    for (const ReadDesc& r : b->reads) total += r.n_bands;
+    if (threshold <= 0) threshold = std::max<int64_t>(1, total / std::max(1, blocks * 4));
+    int n = 0;
+    for (int32_t i : b->order) {
+        if (n >= blocks || b->reads[(size_t)i].n_bands < threshold) break;
+        ++n;
+    }
+    return n;
+}
+
 // Queues pre, core and post for a batch on the context's stream.
 static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches) {
     LaunchArgs la;
-    la.reads = b->d_reads;
-    la.n_reads = b->n_reads;
-    la.g = global_consts(0);
-    la.seq = b->d_seq;
-    la.ev_in = b->d_ev;
-    la.model = b->d_model;
-    la.ev_mean = b->d_ev_mean;
-    la.km_gm = b->d_km_gm;
-    la.km_sd = b->d_km_sd;
-    la.km_k1 = b->d_km_k1;
-    la.last_col = b->d_last_col;
-    la.trace = b->d_trace;
-    la.scores = b->scores_kept ? b->d_scores : nullptr;
-    la.band_k0 = b->d_band_k0;
-    la.pairs = b->d_pairs;
-    la.n_pairs = b->d_n_pairs;
-    la.best = b->d_best;
-    la.status = b->d_status;
-    la.slow = b->d_slow;
-    la.order = b->d_order;
-    la.queue = b->d_queue;
-    la.n_wide = b->n_wide;
+    const GlobalConsts g = global_consts(0);
+    la.pre = PreArgs{b->d_reads, b->n_reads, g, b->d_seq, b->d_ev, b->d_model, b->d_ev_mean, b->d_km_gm,
+                     b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col};
+    la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
+                       b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
+                       b->d_slow, b->d_order, b->d_queue, b->n_wide};
+    la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1,
+                       b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
+                       b->d_status};
     la.sm_count = c->sm_count;
-    la.spin_limit = (int32_t)std::min<int64_t>(c->spin_limit, 0x7fffffff);
     la.stream = c->stream;
     la.ev_pre = c->ev[1];
     la.ev_core = c->ev[2];
-    cudaError_t e = c->mode == ABEA_MODE_BATCHED ? launch_batched(la, launches)
-                                                 : launch_plain(la, launches);
+    cudaError_t e = c->mode == ABEA_MODE_BATCHED ? launch_batched(la, launches) : launch_plain(la, launches);
     if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
     return ABEA_OK;
 }
@@ -492,8 +512,9 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
     }
     // wide shape for the longest reads in the batched form
     b->n_wide = 0;
-    if (c->mode == ABEA_MODE_BATCHED) b->n_wide = choose_wide_reads(b->reads, b->order, c->sm_count, c->long_read_bands);
-    CUDA_TRY(cudaMemsetAsync(b->d_slow, 0, sizeof(unsigned long long), c->stream));
+    if (c->mode == ABEA_MODE_BATCHED)
+        b->n_wide = choose_wide_reads(b, c->sm_count, c->long_read_bands, b->scores_kept);
+    CUDA_TRY(cudaMemsetAsync(b->d_slow, 0, sizeof(unsigned long long) * 4, c->stream));
     CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int32_t) * 8, c->stream));
     CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
     int launches = 0;

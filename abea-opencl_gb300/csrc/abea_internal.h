@@ -6,8 +6,9 @@
 //   ev_in               abea_event_t[sum n_events] as given (24 B/event)
 //   model               abea_model_t[4096]
 //   ev_mean             f32 [per read: round_up(n_events,16)]   event means (pre)
-//   km_gm/km_sd/km_k1   f32 [per read: round_up(n_kmers,16)]    scaled level mean,
-//                       level stdv, (log_inv_sqrt_2pi - log stdv) per k-mer position (pre)
+//   km_gm/km_sd/km_rsd/km_k1  f32 [per read: round_up(n_kmers,16)]  scaled level mean,
+//                       level stdv, RN(1/stdv), (log_inv_sqrt_2pi - log stdv) per
+//                       k-mer position (pre)
 //   last_col            f32 [per read: round_up(n_events,16)]   scores of the last
 //                       k-mer column, -inf where the cell was not computed (core)
 //   trace               u8  [per read: round_up(n_bands,4) * 128]  backpointers,
@@ -52,7 +53,7 @@ struct ReadDesc {
     float em_floor;     // largest power of two <= max(|step_h|, |stay_h|)
     float b_max;        // max(|step_h|, |stay_h|)
     int32_t skip;       // 1: nothing to align (n_kmers <= 0 or n_events <= 0)
-    int32_t pad_;
+    int32_t nonpos;     // 1: every emission of this read is <= 0 (see abea_cell.cuh)
 };
 
 struct GlobalConsts {

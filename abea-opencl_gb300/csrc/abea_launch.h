@@ -1,4 +1,5 @@
-// abea_launch.h — kernel launch entry points used by the host orchestration.
+// abea_launch.h — kernel arguments and launch entry points used by the host
+// orchestration (abea_host.cu) and defined in abea_kernels.cu.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -8,7 +9,7 @@
 
 namespace abea {
 
-struct LaunchArgs {
+struct PreArgs {
     const ReadDesc* reads;
     int n_reads;
     GlobalConsts g;
@@ -18,32 +19,62 @@ struct LaunchArgs {
     float* ev_mean;
     float* km_gm;
     float* km_sd;
+    float* km_rsd;
     float* km_k1;
     float* last_col;
+};
+
+struct CoreArgs {
+    const ReadDesc* reads;
+    int n_reads;
+    GlobalConsts g;
+    const float* ev_mean;
+    const float* km_gm;
+    const float* km_sd;
+    const float* km_rsd;
+    const float* km_k1;
+    float* last_col;
     uint8_t* trace;
-    float* scores;  // nullptr: scores not kept
+    float* scores;                 // nullptr: scores not kept
     int32_t* band_k0;
+    unsigned long long* counters;  // [0] cells on the FP64 tier, [1] cells on the exact-all tier
+    const int32_t* order;          // read indices, longest first
+    int32_t* queue;                // zeroed work counters of the batched form
+    int32_t n_wide;                // leading reads of `order` that run on the wide shape
+};
+
+struct PostArgs {
+    const ReadDesc* reads;
+    int n_reads;
+    GlobalConsts g;
+    const float* ev_mean;
+    const float* km_gm;
+    const float* km_sd;
+    const float* km_k1;
+    const float* last_col;
+    const uint8_t* trace;
+    const int32_t* band_k0;
     abea_aligned_pair_t* pairs;
     int32_t* n_pairs;
-    float* best;
-    int32_t* status;
-    unsigned long long* slow;
-    const int32_t* order;  // read indices, longest first
-    int32_t* queue;        // zeroed work counters
-    int32_t n_wide;        // leading reads of `order` that run on the wide shape
+    float* best_scores;
+    int32_t* status;  // per-read abea_status_t (0 = ok)
+};
+
+struct LaunchArgs {
+    PreArgs pre;
+    CoreArgs core;
+    PostArgs post;
     int sm_count;
-    int32_t spin_limit;
     cudaStream_t stream;
     cudaEvent_t ev_pre;   // recorded after pre
-    cudaEvent_t ev_core;  // recorded after core
+    cudaEvent_t ev_core;  // recorded after core (batched: after the fused core+post)
 };
 
 // Plain form: pre, core, post — one block per read each, as the reference.
 cudaError_t launch_plain(const LaunchArgs& a, int* launches);
 // Batched form: pre, then one persistent fused core+post kernel.
 cudaError_t launch_batched(const LaunchArgs& a, int* launches);
-// Number of leading reads of `order` that the batched form runs on the wide shape.
-int choose_wide_reads(const std::vector<ReadDesc>& reads, const std::vector<int32_t>& order, int sm_count,
-                      int64_t long_read_bands);
+// Resident blocks per SM of the batched kernel.
+int batched_blocks_per_sm(bool scores);
 
 }  // namespace abea

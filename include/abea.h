@@ -219,6 +219,13 @@ abea_status_t abea_ctx_elapsed(abea_ctx_t *ctx, int from_marker, int to_marker, 
  * context's stream (benchmark hygiene between timed runs). */
 abea_status_t abea_ctx_flush_l2(abea_ctx_t *ctx);
 
+/* Self-test of the kernels' exact FP32 arithmetic on the current device:
+ * `cases` pseudo-random and near-rounding-midpoint cases of the division and
+ * of the double-rounded sums, checked against IEEE division and FP64 adds.
+ * out[5]: division wrong, division declined, sum wrong, sum declined, cases.
+ * "wrong" must be 0; "declined" cases take the FP64 path in the kernels. */
+abea_status_t abea_selftest_arith(int64_t cases, uint64_t seed, int64_t *out);
+
 #ifdef __cplusplus
 }
 #endif

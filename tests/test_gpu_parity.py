@@ -160,3 +160,34 @@ def test_empty_batch(lib):
     b = synth.make_batch("small", seed=1).subset([])
     _, pairs, counts = run(b)
     assert len(counts) == 0
+
+
+def test_exact_arithmetic_selftest(lib):
+    """The FP32 division and double-rounded sums never claim a wrong result on
+    2^28 random and near-midpoint cases; declines stay rare."""
+    r = abea.selftest_arith(1 << 28, seed=12345)
+    assert r["div_wrong"] == 0
+    assert r["sum_wrong"] == 0
+    assert r["div_declined"] < r["cases"] * 1e-3
+    # half the sums aim at rounding midpoints on purpose
+    assert r["sum_declined"] < r["cases"] * 0.6
+
+
+@pytest.mark.parametrize("mode", [abea.MODE_PLAIN, abea.MODE_BATCHED])
+def test_f5c_batch_full_size(lib, oracle_mod, mode):
+    """The whole benchmark workload (1.3 Mbases, ~360 reads), bit-exact."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("f5c_batch", seed=1)
+    _, gp, gc = run(batch, mode)
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
+
+
+def test_uneven_batch_batched_equals_plain(lib):
+    """Heavy-tailed 1.3 Mbase batch: batched (wide + warp shapes, fused post) and
+    plain forms give identical AlignedPairs."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("uneven", seed=2)
+    _, p1, c1 = run(batch, abea.MODE_PLAIN)
+    _, p2, c2 = run(batch, abea.MODE_BATCHED)
+    assert_same_alignments(batch, p2, c2, p1, c1)
