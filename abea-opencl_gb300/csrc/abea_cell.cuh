@@ -6,17 +6,18 @@
 //     l = (float)( (double)left + lp_skip)
 // then keeps the largest with U winning ties over D and L over both.  GB300 runs
 // FP64 adds and f32<->f64 conversions at ~1/70 of the FP32 rate, so a cell is
-// evaluated in FP32 in three tiers, every tier bit-exact:
+// evaluated in FP32, bit-exactly:
 //
-//  1. fast: the three candidates are approximated in plain FP32 (error < 2^-22
-//     relative when no term is positive, which holds for every pore model whose
-//     log_inv_sqrt_2pi - log(stdv) is <= 0).  When one candidate beats both others
-//     by more than 2^-19 of their magnitude, the reference's comparison outcome
-//     is certain and only the winner is evaluated exactly (exact_sum).
-//  2. medium: otherwise all three are evaluated with exact_sum and compared.
-//  3. slow: if any exact_sum cannot prove its result (or the emission's
-//     division cannot), the cell is recomputed with native FP64 and IEEE
-//     division, literally as the reference does.
+//  * d and u are evaluated exactly with exact_sum (below) and compared exactly;
+//    they depend only on the previous bands, so the kernels compute them before
+//    the band's exchange of neighbour cells (off the band-to-band critical path);
+//  * l is approximated in plain FP32 (error < 2^-22 relative when no term is
+//    positive, which holds for every pore model whose log_inv_sqrt_2pi -
+//    log(stdv) is <= 0); when it is below max(d, u) by more than 2^-19 of its
+//    magnitude it can neither win nor tie; otherwise it is evaluated exactly too;
+//  * the emission's division uses a reciprocal and a proven correction step;
+//  * if any exactness proof does not go through, the cell is recomputed with
+//    native FP64 and IEEE division, literally as the reference does (cell_slow).
 //
 // exact_sum(a, B, c) returns RN32(RN64(RN64(a + B) + c)) for floats a, c and a
 // double B = bh + bl + r (bh = RN32(B), bl = RN32(B - bh), |r| <= 2^-48|B|):
@@ -43,7 +44,7 @@ namespace abea {
 
 constexpr float kLogInvSqrt2Pi = -0.918938f;           // GPU/align_cuda.cl:66
 constexpr float kErrScale = 2.2737367544323206e-13f;   // 2^-42
-constexpr float kClear = 0.99999809265136719f;         // 1 - 2^-19
+constexpr float kBelow = 1.0000019073486328f;          // 1 + 2^-19
 constexpr float kDivHi = 1.0000009536743164f;          // 1 + 2^-20
 constexpr float kDivLo = 0.99999904632568359f;         // 1 - 2^-20
 constexpr float kTiny = 7.8886090522101181e-31f;       // 2^-100
@@ -122,50 +123,52 @@ __device__ __forceinline__ float pick(float d, float u, float l, uint32_t& from)
     return best;
 }
 
-// Tier 1.  Returns the cell score; tier = 0 when done, 1 when the medium tier
-// must decide, 2 when the slow tier must recompute.
-__device__ __forceinline__ float cell_fast(float diag, float up, float left, float x, float gm, float sd,
-                                           float rsd, float k1, const CellConsts& c, uint32_t& from,
-                                           int& tier, float& em) {
-    bool div_ok;
+// Phase A of a cell: everything that does not need the band's exchange —
+// the emission and the exact diagonal (D) and up (U) candidates.
+__device__ __forceinline__ void cell_du(float diag, float up, float x, float gm, float sd, float rsd, float k1,
+                                        const CellConsts& c, float& d, float& u, float& em, bool& ok) {
+    bool div_ok, okd, oku;
     em = emission_fast(x, gm, sd, rsd, k1, div_ok);
-    // approximations, error < 2^-22 of their magnitude when no term is positive
-    float dA = __fadd_rn(__fadd_rn(diag, c.step_h), em);
-    float uA = __fadd_rn(__fadd_rn(up, c.stay_h), em);
-    float lA = __fadd_rn(left, c.skip_h);
-    float tD = __fmul_rn(dA, kClear), tU = __fmul_rn(uA, kClear), tL = __fmul_rn(lA, kClear);
-    bool winD = (dA > tU) && (dA > tL);
-    bool winU = (uA > tD) && (uA > tL);
-    bool winL = (lA > tD) && (lA > tU);
-    bool all_inf = (diag == -INFINITY) && (up == -INFINITY) && (left == -INFINITY);
-    float a = winD ? diag : (winU ? up : left);
-    float bh = winD ? c.step_h : (winU ? c.stay_h : c.skip_h);
-    float bl = winD ? c.step_l : (winU ? c.stay_l : c.skip_l);
-    float cc = winL ? 0.0f : em;
-    bool c_ok = winL || (fabsf(em) >= c.em_floor);
-    from = winD ? ABEA_FROM_D : (winU ? ABEA_FROM_U : ABEA_FROM_L);
-    bool ok;
-    float v = exact_sum(a, bh, bl, cc, c_ok, ok);
-    bool decided = c.nonpos && (winD || winU || winL);
-    tier = all_inf ? 0 : (!div_ok ? 2 : (!decided ? 1 : (ok ? 0 : 2)));
-    return all_inf ? -INFINITY : v;
+    const bool c_ok = fabsf(em) >= c.em_floor;
+    d = exact_sum_inf(diag, c.step_h, c.step_l, em, c_ok, okd);
+    u = exact_sum_inf(up, c.stay_h, c.stay_l, em, c_ok, oku);
+    ok = div_ok && okd && oku;
 }
 
-// Tier 2: all three candidates exactly, then the reference's comparison.
-__device__ __forceinline__ float cell_medium(float diag, float up, float left, float em, const CellConsts& c,
-                                             uint32_t& from, bool& ok) {
-    bool c_ok = fabsf(em) >= c.em_floor;
-    bool okd, oku, okl;
-    float d = exact_sum_inf(diag, c.step_h, c.step_l, em, c_ok, okd);
-    float u = exact_sum_inf(up, c.stay_h, c.stay_l, em, c_ok, oku);
-    float l = exact_sum_inf(left, c.skip_h, c.skip_l, 0.0f, true, okl);
-    ok = okd && oku && okl;
+// max(d, u) with U winning ties (no L candidate).
+__device__ __forceinline__ float pick_du(float d, float u, uint32_t& from) {
+    float best = u > d ? u : d;
+    from = (best == u) ? ABEA_FROM_U : ABEA_FROM_D;
+    return best;
+}
+
+// Phase B: the skip (L) candidate.  When every term is <= 0 and the plain-FP32
+// approximation of l is below max(d, u) by more than 2^-19 of its magnitude
+// (its error is < 2^-22 of it), l can neither win nor tie and need not be
+// evaluated exactly.  All-(-inf) cells resolve to -inf, FROM_L (tie rule).
+// Returns need_l = true when l must be evaluated exactly (cell_l).
+__device__ __forceinline__ float cell_b(float d, float u, float left, const CellConsts& c, uint32_t& from,
+                                        bool& need_l) {
+    const float mx = u > d ? u : d;
+    const float lA = __fadd_rn(left, c.skip_h);
+    const bool below = c.nonpos && (lA < __fmul_rn(mx, kBelow));
+    const bool all_inf = (mx == -INFINITY) && (left == -INFINITY) && (d == -INFINITY);
+    need_l = !below && !all_inf;
+    float best = pick_du(d, u, from);
+    if (all_inf) from = ABEA_FROM_L;
+    return best;
+}
+
+// Exact L candidate and the reference's three-way comparison.
+__device__ __forceinline__ float cell_l(float d, float u, float left, const CellConsts& c, uint32_t& from, bool& ok) {
+    const float l = exact_sum_inf(left, c.skip_h, c.skip_l, 0.0f, true, ok);
     return pick(d, u, l, from);
 }
 
-// Tier 3: the reference's arithmetic verbatim (IEEE division, FP64 adds).
-__device__ __forceinline__ float cell_slow(float diag, float up, float left, float x, float gm, float sd,
-                                           float k1, const CellConsts& c, uint32_t& from) {
+// The reference's arithmetic verbatim (IEEE division, FP64 adds): the fallback
+// when an exactness proof does not go through.
+static __device__ __noinline__ float cell_slow(float diag, float up, float left, float x, float gm, float sd, float k1,
+                                        const CellConsts c, uint32_t& from) {
     float em = emission_ieee(x, gm, sd, k1);
     float d = __double2float_rn(__dadd_rn(__dadd_rn((double)diag, c.lp_step), (double)em));
     float u = __double2float_rn(__dadd_rn(__dadd_rn((double)up, c.lp_stay), (double)em));

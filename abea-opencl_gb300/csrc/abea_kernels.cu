@@ -196,6 +196,10 @@ __device__ __forceinline__ void band_range(int k0, int e0, int n_events, int n_k
 }
 
 // ---------------------------------------------------------------- warp shape
+// Slot s of a band holds the cell of k-mer k(s) = k0 + ((s - k0) & 127) and event
+// e = (band - 2) - k(s).  A slot inside band b keeps its k-mer from band b-1, so
+// its event advances by one and its emission and its D and U candidates can be
+// computed from band b-1 alone, before band b's placement is known.
 template <bool kScores>
 __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int lane) {
     const CellConsts cc = make_consts(r, a.g);
@@ -213,8 +217,12 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
     // band 0: start cell (e=-1,k=-1) = 0 in slot 127; band 1: trim cell (e=0,k=-1)
     // = (float)lp_trim, FROM_U, slot 127 (GPU/align_cuda.cl:249-268).
     float S1[4], LP[4];
+    int et[4];  // event of each slot under the previous band's placement
 #pragma unroll
-    for (int j = 0; j < 4; ++j) S1[j] = LP[j] = -INFINITY;
+    for (int j = 0; j < 4; ++j) {
+        S1[j] = LP[j] = -INFINITY;
+        et[j] = e0 - ((4 * lane + j - k0) & 127);
+    }
     if (lane == 31) S1[3] = a.g.trim_f;
     if (lane == 0) LP[0] = 0.0f;  // band 0 shifted by one slot = diagonal source of band 2
     if (kScores) {
@@ -224,116 +232,122 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         reinterpret_cast<float4*>(scores + kSlots)[lane] = b1;
     }
     int my_k0 = k0;  // bands 0 and 1 (lanes 0, 1) both have k0 = -51
-    unsigned long long slow = 0, medium = 0;
+    unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
+    uint4 tacc = make_uint4(0u, lane == 31 ? (ABEA_FROM_U << 24) : 0u, 0u, 0u);
 
-    const int n_tiles = (n_bands + 3) >> 2;
-    for (int tile = 0; tile < n_tiles; ++tile) {
-        if (tile > 0 && rings_step(rg, rs, a, r, lane, k0, e0, 4)) __syncwarp();
-        uint32_t tacc[4] = {0u, 0u, 0u, 0u};
-        if (tile == 0) tacc[1] = lane == 31 ? (ABEA_FROM_U << 24) : 0u;
+    for (int b = 2; b < n_bands; ++b) {
+        if ((b & 3) == 0) {
+            if (rings_step(rg, rs, a, r, lane, k0, e0, 4)) __syncwarp();
+        }
+        // ---- exchange: end cells for the placement, left neighbour of slot 4*lane
+        const int sl = k0 & 127, su = (k0 + kBand - 1) & 127;
+        const float ll = __shfl_sync(kFull, sel4(S1, sl & 3), sl >> 2);
+        const float ur = __shfl_sync(kFull, sel4(S1, su & 3), su >> 2);
+        const float left0 = __shfl_sync(kFull, S1[3], (lane + 31) & 31);
+        // ---- phase A (previous placement only): emission, exact D and U
+        const float4 gm4 = *reinterpret_cast<const float4*>(&rg.gm[4 * lane]);
+        const float4 sd4 = *reinterpret_cast<const float4*>(&rg.sd[4 * lane]);
+        const float4 rs4 = *reinterpret_cast<const float4*>(&rg.rsd[4 * lane]);
+        const float4 k14 = *reinterpret_cast<const float4*>(&rg.k1[4 * lane]);
+        const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w};
+        const float sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
+        const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w};
+        const float k1v[4] = {k14.x, k14.y, k14.z, k14.w};
+        float d[4], u[4], em[4], xv[4];
+        bool okA[4];
 #pragma unroll
-        for (int jb = 0; jb < 4; ++jb) {
-            const int b = tile * 4 + jb;
-            if (b < 2) continue;
-            if (b >= n_bands) break;
-            // ---- band placement (Suzuki-Kasahara), GPU/align_cuda.cl:394-430
-            const int sl = k0 & 127, su = (k0 + kBand - 1) & 127;
-            const float ll = __shfl_sync(kFull, sel4(S1, sl & 3), sl >> 2);
-            const float ur = __shfl_sync(kFull, sel4(S1, su & 3), su >> 2);
-            const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
-            k0 += right ? 1 : 0;
-            e0 += right ? 0 : 1;
-            int lo, hi;
-            band_range(k0, e0, n_events, n_kmers, lo, hi);
-
-            float left[4];
-            left[0] = __shfl_sync(kFull, S1[3], (lane + 31) & 31);
-            left[1] = S1[0];
-            left[2] = S1[1];
-            left[3] = S1[2];
-            const float4 gm4 = *reinterpret_cast<const float4*>(&rg.gm[4 * lane]);
-            const float4 sd4 = *reinterpret_cast<const float4*>(&rg.sd[4 * lane]);
-            const float4 rs4 = *reinterpret_cast<const float4*>(&rg.rsd[4 * lane]);
-            const float4 k14 = *reinterpret_cast<const float4*>(&rg.k1[4 * lane]);
-            const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w};
-            const float sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
-            const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w};
-            const float k1v[4] = {k14.x, k14.y, k14.z, k14.w};
-
-            float best[4], em[4], xv[4];
-            uint32_t from[4];
-            int tier[4];
-            bool valid[4];
-            bool any_med = false, any_slow = false;
+        for (int j = 0; j < 4; ++j) {
+            xv[j] = rg.ev[(et[j] + 1) & (kEvRing - 1)];
+            cell_du(LP[j], S1[j], xv[j], gmv[j], sdv[j], rsv[j], k1v[j], cc, d[j], u[j], em[j], okA[j]);
+        }
+        // ---- band placement (Suzuki-Kasahara), GPU/align_cuda.cl:394-430
+        const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
+        k0 += right ? 1 : 0;
+        e0 += right ? 0 : 1;
+        int lo, hi;
+        band_range(k0, e0, n_events, n_kmers, lo, hi);
+        // ---- phase B: the skip candidate, tiers, masking
+        const float left[4] = {left0, S1[0], S1[1], S1[2]};
+        float best[4];
+        uint32_t from[4];
+        bool valid[4], need_l[4], bad[4];
+        bool any_l = false, any_bad = false;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int o = (4 * lane + j - k0) & 127;
-                valid[j] = (o >= lo) && (o < hi);
-                xv[j] = rg.ev[(e0 - o) & (kEvRing - 1)];
-                best[j] = cell_fast(LP[j], S1[j], left[j], xv[j], gmv[j], sdv[j], rsv[j], k1v[j], cc, from[j],
-                                    tier[j], em[j]);
-                tier[j] = valid[j] ? tier[j] : 0;
-                any_med |= tier[j] == 1;
-                any_slow |= tier[j] == 2;
-            }
-            if (__any_sync(kFull, any_med)) {
+        for (int j = 0; j < 4; ++j) {
+            const int o = (4 * lane + j - k0) & 127;
+            et[j] = e0 - o;
+            valid[j] = (o >= lo) && (o < hi);
+            best[j] = cell_b(d[j], u[j], left[j], cc, from[j], need_l[j]);
+            need_l[j] = need_l[j] && valid[j];
+            bad[j] = valid[j] && !okA[j];
+            any_l |= need_l[j];
+        }
+        if (__any_sync(kFull, any_l)) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (tier[j] == 1) {
-                        bool ok;
-                        best[j] = cell_medium(LP[j], S1[j], left[j], em[j], cc, from[j], ok);
-                        tier[j] = ok ? 0 : 2;
-                        any_slow |= !ok;
-                        ++medium;
-                    }
-            }
-            if (__any_sync(kFull, any_slow)) {
+            for (int j = 0; j < 4; ++j)
+                if (need_l[j]) {
+                    bool ok;
+                    best[j] = cell_l(d[j], u[j], left[j], cc, from[j], ok);
+                    bad[j] |= !ok;
+                }
+        }
 #pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    if (tier[j] == 2) {
-                        best[j] = cell_slow(LP[j], S1[j], left[j], xv[j], gmv[j], sdv[j], k1v[j], cc, from[j]);
-                        ++slow;
-                    }
-            }
-            uint32_t word = 0;
+        for (int j = 0; j < 4; ++j) any_bad |= bad[j];
+        if (__any_sync(kFull, any_bad)) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                best[j] = valid[j] ? best[j] : -INFINITY;
-                word |= (valid[j] ? from[j] : 0u) << (8 * j);
-            }
-            // trim cell (k = -1, slot 127), GPU/align_cuda.cl:431-443
-            if (k0 <= -1 && k0 >= -kBand && lane == 31) {
-                const int et = e0 + 1 + k0;
-                const bool in = et >= 0 && et < n_events;
-                best[3] = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(et + 1))) : -INFINITY;
+            for (int j = 0; j < 4; ++j)
+                if (bad[j]) {
+                    best[j] = cell_slow(LP[j], S1[j], left[j], xv[j], gmv[j], sdv[j], k1v[j], cc, from[j]);
+                    ++slow;
+                }
+        }
+        uint32_t word = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            best[j] = valid[j] ? best[j] : -INFINITY;
+            word |= (valid[j] ? from[j] : 0u) << (8 * j);
+        }
+        // trim cell (k = -1, slot 127), GPU/align_cuda.cl:431-443
+        if (k0 <= -1 && k0 >= -kBand) {
+            if (lane == 31) {
+                const int e_t = e0 + 1 + k0;
+                const bool in = e_t >= 0 && e_t < n_events;
+                best[3] = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
                 word = (word & 0x00ffffffu) | (in ? (ABEA_FROM_U << 24) : 0u);
             }
-            // last k-mer column, consumed by the post stage (GPU/align_cuda.cl:722-746)
-            {
-                const int ol = n_kmers - 1 - k0;
-                if (ol >= lo && ol < hi && lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                LP[j] = left[j];
-                S1[j] = best[j];
-            }
-            tacc[jb] = word;
-            if (kScores)
-                reinterpret_cast<float4*>(scores + (int64_t)b * kSlots)[lane] =
-                    make_float4(best[0], best[1], best[2], best[3]);
-            if ((b & 31) == lane) my_k0 = k0;
-            if ((b & 31) == 31 || b == n_bands - 1) {
-                if (lane <= (b & 31)) bk0[(b & ~31) + lane] = my_k0;
+        }
+        // last k-mer column, consumed by the post stage (GPU/align_cuda.cl:722-746)
+        {
+            const int ol = n_kmers - 1 - k0;
+            if (ol >= lo && ol < hi) {
+                if (lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
             }
         }
-        reinterpret_cast<uint4*>(trace + (int64_t)tile * 512)[lane] = make_uint4(tacc[0], tacc[1], tacc[2], tacc[3]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            LP[j] = left[j];
+            S1[j] = best[j];
+        }
+        const int jb = b & 3;
+        tacc.x = jb == 0 ? word : tacc.x;
+        tacc.y = jb == 1 ? word : tacc.y;
+        tacc.z = jb == 2 ? word : tacc.z;
+        tacc.w = jb == 3 ? word : tacc.w;
+        if (jb == 3 || b == n_bands - 1) {
+            reinterpret_cast<uint4*>(trace + (int64_t)(b >> 2) * 512)[lane] = tacc;
+            tacc = make_uint4(0u, 0u, 0u, 0u);
+        }
+        if (kScores)
+            reinterpret_cast<float4*>(scores + (int64_t)b * kSlots)[lane] = make_float4(best[0], best[1], best[2], best[3]);
+        if ((b & 31) == lane) my_k0 = k0;
+        if ((b & 31) == 31 || b == n_bands - 1) {
+            if (lane <= (b & 31)) bk0[(b & ~31) + lane] = my_k0;
+        }
     }
     cp_async_wait_all();  // no copy may land in shared memory after the read is done
     __syncwarp();
     if (slow) atomicAdd(&a.counters[0], slow);
-    if (medium) atomicAdd(&a.counters[1], medium);
 }
 
 // ---------------------------------------------------------------- wide shape
@@ -361,6 +375,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     // bands 0 and 1 (trace tile 0: band 1, slot 127 = FROM_U)
     float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // my slot, band 1
     float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
+    int et = e0 - ((t - k0) & 127);                      // my event under band 1's placement
     ws.sc[1][t] = s_prev;
     ws.tile[0][t] = 0u;
     ws.tile[1][t] = 0u;
@@ -372,50 +387,59 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     __syncthreads();
     if (t == 0) tile_bytes[(127 >> 2) * 16 + 1 * 4 + (127 & 3)] = (uint8_t)ABEA_FROM_U;
     __syncthreads();
-    unsigned long long slow = 0, medium = 0;
+    unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
 
     for (int b = 2; b < n_bands; ++b) {
         const int pb = (b - 1) & 1;
-        // ---- band placement from the previous band's end cells
+        // ---- exchange (shared memory, written before the previous barrier)
         const float ll = ws.sc[pb][k0 & 127];
         const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
         const float left = ws.sc[pb][(t + 127) & 127];
+        // ---- phase A (previous placement only)
+        const float x = ws.rg.ev[(et + 1) & (kEvRing - 1)];
+        const float gmt = ws.rg.gm[t], sdt = ws.rg.sd[t], rst = ws.rg.rsd[t], k1t = ws.rg.k1[t];
+        float d, u, em;
+        bool okA;
+        cell_du(lp, s_prev, x, gmt, sdt, rst, k1t, cc, d, u, em, okA);
+        // ---- placement
         const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
         k0 += right ? 1 : 0;
         e0 += right ? 0 : 1;
         int lo, hi;
         band_range(k0, e0, n_events, n_kmers, lo, hi);
         const int o = (t - k0) & 127;
+        et = e0 - o;
         const bool valid = (o >= lo) && (o < hi);
-        const float x = ws.rg.ev[(e0 - o) & (kEvRing - 1)];
-        const float gm = ws.rg.gm[t], sd = ws.rg.sd[t], rsd = ws.rg.rsd[t], k1 = ws.rg.k1[t];
+        // ---- phase B
         uint32_t from;
-        int tier;
-        float em;
-        float best = cell_fast(lp, s_prev, left, x, gm, sd, rsd, k1, cc, from, tier, em);
-        tier = valid ? tier : 0;
-        if (tier == 1) {
+        bool need_l;
+        float best = cell_b(d, u, left, cc, from, need_l);
+        bool bad = valid && !okA;
+        if (need_l && valid) {
             bool ok;
-            best = cell_medium(lp, s_prev, left, em, cc, from, ok);
-            tier = ok ? 0 : 2;
-            ++medium;
+            best = cell_l(d, u, left, cc, from, ok);
+            bad |= !ok;
         }
-        if (tier == 2) {
-            best = cell_slow(lp, s_prev, left, x, gm, sd, k1, cc, from);
+        if (bad) {
+            best = cell_slow(lp, s_prev, left, x, gmt, sdt, k1t, cc, from);
             ++slow;
         }
         best = valid ? best : -INFINITY;
         from = valid ? from : 0u;
-        if (t == 127 && k0 <= -1 && k0 >= -kBand) {  // trim cell (k = -1)
-            const int et = e0 + 1 + k0;
-            const bool in = et >= 0 && et < n_events;
-            best = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(et + 1))) : -INFINITY;
-            from = in ? ABEA_FROM_U : 0u;
+        if (k0 <= -1 && k0 >= -kBand) {  // trim cell (k = -1, slot 127)
+            if (t == 127) {
+                const int e_t = e0 + 1 + k0;
+                const bool in = e_t >= 0 && e_t < n_events;
+                best = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
+                from = in ? ABEA_FROM_U : 0u;
+            }
         }
-        if (t == sl_last) {
+        {
             const int ol = n_kmers - 1 - k0;
-            if (ol >= lo && ol < hi) lastc[e0 - ol] = best;
+            if (ol >= lo && ol < hi) {
+                if (t == sl_last) lastc[e0 - ol] = best;
+            }
         }
         lp = left;
         s_prev = best;
@@ -438,7 +462,6 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     cp_async_wait_all();
     __syncthreads();
     if (slow) atomicAdd(&a.counters[0], slow);
-    if (medium) atomicAdd(&a.counters[1], medium);
 }
 
 // ---------------------------------------------------------------- post
