@@ -21,7 +21,8 @@
 //
 // exact_sum(a, B, c) returns RN32(RN64(RN64(a + B) + c)) for floats a, c and a
 // double B = bh + bl + r (bh = RN32(B), bl = RN32(B - bh), |r| <= 2^-48|B|):
-// Fast2Sum (Dekker 1971) gives p + q = c + bh and s + e = a + p exactly, the
+// TwoSum (Knuth) gives p + q = c + bh and Fast2Sum (Dekker 1971) s + e = a + p
+// exactly, the
 // exact sum a + B + c lies within eb = 2^-42 (|a| + |c| + |bh|) of s + t with
 // t = e + (q + bl) (eb also covers the reference's own two double roundings,
 // each <= 2^-53 of the same magnitudes), and RN32(s + (t + eb)) ==
@@ -51,8 +52,7 @@ constexpr float kTiny = 7.8886090522101181e-31f;       // 2^-100
 
 struct CellConsts {
     float step_h, step_l, stay_h, stay_l, skip_h, skip_l;
-    float em_floor;  // power of two <= max(|step_h|, |stay_h|): Fast2Sum(em, Bh) precondition
-    int nonpos;      // every emission of this read is <= 0 (tier 1 allowed)
+    int nonpos;      // every emission of this read is <= 0 (the skip shortcut is valid)
     double lp_step, lp_stay, lp_skip;
 };
 
@@ -87,25 +87,27 @@ __device__ __forceinline__ float emission_ieee(float x, float gm, float sd, floa
 }
 
 // RN32(RN64(RN64(a + (bh+bl)) + c)) for finite a and c, or ok = false.
-// c_ok: Fast2Sum(c, bh) is exact (c == 0 or exponent(c) >= exponent(bh)).
-__device__ __forceinline__ float exact_sum(float a, float bh, float bl, float c, bool c_ok, bool& ok) {
-    float p = __fadd_rn(c, bh);
-    float q = __fsub_rn(bh, __fsub_rn(p, c));
-    float w = __fadd_rn(q, bl);
-    float s = __fadd_rn(a, p);
-    float e = __fsub_rn(p, __fsub_rn(s, a));
-    float t = __fadd_rn(e, w);
-    float eb = __fmul_rn(__fadd_rn(__fadd_rn(fabsf(a), fabsf(c)), fabsf(bh)), kErrScale);
-    float hp = __fadd_rn(s, __fadd_rn(t, eb));
-    float hm = __fadd_rn(s, __fsub_rn(t, eb));
-    ok = (hp == hm) && (fabsf(a) >= fabsf(p)) && c_ok;
+// p + q = c + bh by TwoSum (Knuth; no precondition), s + e = a + p by Fast2Sum,
+// exact when |a| >= |p| (checked: fails only in a read's first bands).
+__device__ __forceinline__ float exact_sum(float a, float bh, float bl, float c, bool& ok) {
+    const float p = __fadd_rn(c, bh);
+    const float bv = __fsub_rn(p, c);
+    const float q = __fadd_rn(__fsub_rn(c, __fsub_rn(p, bv)), __fsub_rn(bh, bv));
+    const float w = __fadd_rn(q, bl);
+    const float s = __fadd_rn(a, p);
+    const float e = __fsub_rn(p, __fsub_rn(s, a));
+    const float t = __fadd_rn(e, w);
+    const float eb = __fmul_rn(__fadd_rn(__fadd_rn(fabsf(a), fabsf(c)), fabsf(bh)), kErrScale);
+    const float hp = __fadd_rn(s, __fadd_rn(t, eb));
+    const float hm = __fadd_rn(s, __fsub_rn(t, eb));
+    ok = (hp == hm) && (fabsf(a) >= fabsf(p));
     return hp;
 }
 
 // exact_sum that also accepts a = -inf (result -inf, exact for finite c).
-__device__ __forceinline__ float exact_sum_inf(float a, float bh, float bl, float c, bool c_ok, bool& ok) {
+__device__ __forceinline__ float exact_sum_inf(float a, float bh, float bl, float c, bool& ok) {
     bool ok1;
-    float v = exact_sum(a, bh, bl, c, c_ok, ok1);
+    float v = exact_sum(a, bh, bl, c, ok1);
     bool a_inf = a == -INFINITY;
     ok = ok1 || (a_inf && fabsf(c) < INFINITY);
     return a_inf ? -INFINITY : v;
@@ -129,9 +131,8 @@ __device__ __forceinline__ void cell_du(float diag, float up, float x, float gm,
                                         const CellConsts& c, float& d, float& u, float& em, bool& ok) {
     bool div_ok, okd, oku;
     em = emission_fast(x, gm, sd, rsd, k1, div_ok);
-    const bool c_ok = fabsf(em) >= c.em_floor;
-    d = exact_sum_inf(diag, c.step_h, c.step_l, em, c_ok, okd);
-    u = exact_sum_inf(up, c.stay_h, c.stay_l, em, c_ok, oku);
+    d = exact_sum_inf(diag, c.step_h, c.step_l, em, okd);
+    u = exact_sum_inf(up, c.stay_h, c.stay_l, em, oku);
     ok = div_ok && okd && oku;
 }
 
@@ -161,7 +162,7 @@ __device__ __forceinline__ float cell_b(float d, float u, float left, const Cell
 
 // Exact L candidate and the reference's three-way comparison.
 __device__ __forceinline__ float cell_l(float d, float u, float left, const CellConsts& c, uint32_t& from, bool& ok) {
-    const float l = exact_sum_inf(left, c.skip_h, c.skip_l, 0.0f, true, ok);
+    const float l = exact_sum_inf(left, c.skip_h, c.skip_l, 0.0f, ok);
     return pick(d, u, l, from);
 }
 

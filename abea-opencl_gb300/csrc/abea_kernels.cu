@@ -65,7 +65,6 @@ __device__ __forceinline__ CellConsts make_consts(const ReadDesc& r, const Globa
     c.stay_l = r.stay_l;
     c.skip_h = g.skip_h;
     c.skip_l = g.skip_l;
-    c.em_floor = r.em_floor;
     c.nonpos = r.nonpos;
     c.lp_step = r.lp_step;
     c.lp_stay = r.lp_stay;
