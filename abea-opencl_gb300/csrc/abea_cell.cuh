@@ -125,15 +125,57 @@ __device__ __forceinline__ float pick(float d, float u, float l, uint32_t& from)
     return best;
 }
 
-// Phase A of a cell: everything that does not need the band's exchange —
-// the emission and the exact diagonal (D) and up (U) candidates.
-__device__ __forceinline__ void cell_du(float diag, float up, float x, float gm, float sd, float rsd, float k1,
-                                        const CellConsts& c, float& d, float& u, float& em, bool& ok) {
-    bool div_ok, okd, oku;
-    em = emission_fast(x, gm, sd, rsd, k1, div_ok);
-    d = exact_sum_inf(diag, c.step_h, c.step_l, em, okd);
-    u = exact_sum_inf(up, c.stay_h, c.stay_l, em, oku);
-    ok = div_ok && okd && oku;
+// Emission-side half of exact_sum: p + q = em + bh by TwoSum, w = q + bl.
+struct EmSplit {
+    float p, w;
+};
+__device__ __forceinline__ EmSplit em_split(float em, float bh, float bl) {
+    EmSplit r;
+    r.p = __fadd_rn(em, bh);
+    const float bv = __fsub_rn(r.p, em);
+    const float q = __fadd_rn(__fsub_rn(em, __fsub_rn(r.p, bv)), __fsub_rn(bh, bv));
+    r.w = __fadd_rn(q, bl);
+    return r;
+}
+
+// Score-side half: RN32(RN64(RN64(a + B) + em)) from a and the emission split;
+// a = -inf gives -inf.  `mag` = |em| + |bh|.  ok = false when not proven.
+__device__ __forceinline__ float exact_from_split(float a, EmSplit sp, float mag, bool em_finite, bool& ok) {
+    const float s = __fadd_rn(a, sp.p);
+    const float e = __fsub_rn(sp.p, __fsub_rn(s, a));
+    const float t = __fadd_rn(e, sp.w);
+    const float eb = __fmul_rn(__fadd_rn(fabsf(a), mag), kErrScale);
+    const float hp = __fadd_rn(s, __fadd_rn(t, eb));
+    const float hm = __fadd_rn(s, __fsub_rn(t, eb));
+    const bool a_inf = a == -INFINITY;
+    ok = ((hp == hm) && (fabsf(a) >= fabsf(sp.p))) || (a_inf && em_finite);
+    return a_inf ? -INFINITY : hp;
+}
+
+// The next band's emission of a slot and the split for its up candidate; the
+// exact diagonal candidate once its diagonal score is known.
+struct NextCell {
+    float em;         // emission
+    EmSplit su;       // em + stay, for u
+    float d;          // exact diagonal candidate
+    bool ok;          // division and d proven
+};
+__device__ __forceinline__ NextCell next_cell(float diag, float x, float gm, float sd, float rsd, float k1,
+                                              const CellConsts& c) {
+    NextCell n;
+    bool div_ok, okd;
+    n.em = emission_fast(x, gm, sd, rsd, k1, div_ok);
+    const bool fin = fabsf(n.em) < INFINITY;
+    const EmSplit sd_ = em_split(n.em, c.step_h, c.step_l);
+    n.d = exact_from_split(diag, sd_, __fadd_rn(fabsf(n.em), fabsf(c.step_h)), fin, okd);
+    n.su = em_split(n.em, c.stay_h, c.stay_l);
+    n.ok = div_ok && okd;
+    return n;
+}
+
+// The up candidate from the previous band's score of the same slot.
+__device__ __forceinline__ float cell_u(float up, const NextCell& n, const CellConsts& c, bool& ok) {
+    return exact_from_split(up, n.su, __fadd_rn(fabsf(n.em), fabsf(c.stay_h)), fabsf(n.em) < INFINITY, ok);
 }
 
 // max(d, u) with U winning ties (no L candidate).

@@ -196,9 +196,12 @@ __device__ __forceinline__ void band_range(int k0, int e0, int n_events, int n_k
 
 // ---------------------------------------------------------------- warp shape
 // Slot s of a band holds the cell of k-mer k(s) = k0 + ((s - k0) & 127) and event
-// e = (band - 2) - k(s).  A slot inside band b keeps its k-mer from band b-1, so
-// its event advances by one and its emission and its D and U candidates can be
-// computed from band b-1 alone, before band b's placement is known.
+// e = (band - 2) - k(s).  A slot inside band b+1 has kept its k-mer since band
+// b-1, so its event is two more than under band b-1's placement: the emission of
+// band b+1 and its exact diagonal candidate (diagonal = left neighbour of band b)
+// are computed during band b, before band b's own placement is decided.  Band b
+// itself then only needs its up candidate (from the slot's own previous score),
+// the exchange of neighbour cells, the skip candidate and the comparison.
 template <bool kScores>
 __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int lane) {
     const CellConsts cc = make_consts(r, a.g);
@@ -216,11 +219,11 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
     // band 0: start cell (e=-1,k=-1) = 0 in slot 127; band 1: trim cell (e=0,k=-1)
     // = (float)lp_trim, FROM_U, slot 127 (GPU/align_cuda.cl:249-268).
     float S1[4], LP[4];
-    int et[4];  // event of each slot under the previous band's placement
+    int ep[4];  // event of each slot under the previous band's placement
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         S1[j] = LP[j] = -INFINITY;
-        et[j] = e0 - ((4 * lane + j - k0) & 127);
+        ep[j] = e0 - ((4 * lane + j - k0) & 127);
     }
     if (lane == 31) S1[3] = a.g.trim_f;
     if (lane == 0) LP[0] = 0.0f;  // band 0 shifted by one slot = diagonal source of band 2
@@ -230,6 +233,18 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         reinterpret_cast<float4*>(scores)[lane] = b0;
         reinterpret_cast<float4*>(scores + kSlots)[lane] = b1;
     }
+    NextCell nc[4];  // band b's emission side, prepared during band b-1
+    {
+        const float4 gm4 = *reinterpret_cast<const float4*>(&rg.gm[4 * lane]);
+        const float4 sd4 = *reinterpret_cast<const float4*>(&rg.sd[4 * lane]);
+        const float4 rs4 = *reinterpret_cast<const float4*>(&rg.rsd[4 * lane]);
+        const float4 k14 = *reinterpret_cast<const float4*>(&rg.k1[4 * lane]);
+        const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w}, sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
+        const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w}, k1v[4] = {k14.x, k14.y, k14.z, k14.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            nc[j] = next_cell(LP[j], rg.ev[(ep[j] + 1) & (kEvRing - 1)], gmv[j], sdv[j], rsv[j], k1v[j], cc);
+    }
     int my_k0 = k0;  // bands 0 and 1 (lanes 0, 1) both have k0 = -51
     unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
@@ -237,37 +252,37 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 
     for (int b = 2; b < n_bands; ++b) {
         if ((b & 3) == 0) {
-            if (rings_step(rg, rs, a, r, lane, k0, e0, 4)) __syncwarp();
+            if (rings_step(rg, rs, a, r, lane, k0, e0, 6)) __syncwarp();
         }
         // ---- exchange: end cells for the placement, left neighbour of slot 4*lane
         const int sl = k0 & 127, su = (k0 + kBand - 1) & 127;
         const float ll = __shfl_sync(kFull, sel4(S1, sl & 3), sl >> 2);
         const float ur = __shfl_sync(kFull, sel4(S1, su & 3), su >> 2);
         const float left0 = __shfl_sync(kFull, S1[3], (lane + 31) & 31);
-        // ---- phase A (previous placement only): emission, exact D and U
+        const float left[4] = {left0, S1[0], S1[1], S1[2]};
+        // ---- up candidates of band b
+        float u[4];
+        bool oku[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) u[j] = cell_u(S1[j], nc[j], cc, oku[j]);
+        // ---- band b+1's emission side (placement-independent)
         const float4 gm4 = *reinterpret_cast<const float4*>(&rg.gm[4 * lane]);
         const float4 sd4 = *reinterpret_cast<const float4*>(&rg.sd[4 * lane]);
         const float4 rs4 = *reinterpret_cast<const float4*>(&rg.rsd[4 * lane]);
         const float4 k14 = *reinterpret_cast<const float4*>(&rg.k1[4 * lane]);
-        const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w};
-        const float sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
-        const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w};
-        const float k1v[4] = {k14.x, k14.y, k14.z, k14.w};
-        float d[4], u[4], em[4], xv[4];
-        bool okA[4];
+        const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w}, sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
+        const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w}, k1v[4] = {k14.x, k14.y, k14.z, k14.w};
+        NextCell nn[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            xv[j] = rg.ev[(et[j] + 1) & (kEvRing - 1)];
-            cell_du(LP[j], S1[j], xv[j], gmv[j], sdv[j], rsv[j], k1v[j], cc, d[j], u[j], em[j], okA[j]);
-        }
+        for (int j = 0; j < 4; ++j)
+            nn[j] = next_cell(left[j], rg.ev[(ep[j] + 2) & (kEvRing - 1)], gmv[j], sdv[j], rsv[j], k1v[j], cc);
         // ---- band placement (Suzuki-Kasahara), GPU/align_cuda.cl:394-430
         const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
         k0 += right ? 1 : 0;
         e0 += right ? 0 : 1;
         int lo, hi;
         band_range(k0, e0, n_events, n_kmers, lo, hi);
-        // ---- phase B: the skip candidate, tiers, masking
-        const float left[4] = {left0, S1[0], S1[1], S1[2]};
+        // ---- skip candidate, comparison, tiers
         float best[4];
         uint32_t from[4];
         bool valid[4], need_l[4], bad[4];
@@ -275,11 +290,11 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int o = (4 * lane + j - k0) & 127;
-            et[j] = e0 - o;
+            ep[j] = e0 - o;
             valid[j] = (o >= lo) && (o < hi);
-            best[j] = cell_b(d[j], u[j], left[j], cc, from[j], need_l[j]);
+            best[j] = cell_b(nc[j].d, u[j], left[j], cc, from[j], need_l[j]);
             need_l[j] = need_l[j] && valid[j];
-            bad[j] = valid[j] && !okA[j];
+            bad[j] = valid[j] && !(nc[j].ok && oku[j]);
             any_l |= need_l[j];
         }
         if (__any_sync(kFull, any_l)) {
@@ -287,7 +302,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
             for (int j = 0; j < 4; ++j)
                 if (need_l[j]) {
                     bool ok;
-                    best[j] = cell_l(d[j], u[j], left[j], cc, from[j], ok);
+                    best[j] = cell_l(nc[j].d, u[j], left[j], cc, from[j], ok);
                     bad[j] |= !ok;
                 }
         }
@@ -297,7 +312,8 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 #pragma unroll
             for (int j = 0; j < 4; ++j)
                 if (bad[j]) {
-                    best[j] = cell_slow(LP[j], S1[j], left[j], xv[j], gmv[j], sdv[j], k1v[j], cc, from[j]);
+                    const float x = rg.ev[ep[j] & (kEvRing - 1)];
+                    best[j] = cell_slow(LP[j], S1[j], left[j], x, gmv[j], sdv[j], k1v[j], cc, from[j]);
                     ++slow;
                 }
         }
@@ -327,6 +343,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         for (int j = 0; j < 4; ++j) {
             LP[j] = left[j];
             S1[j] = best[j];
+            nc[j] = nn[j];
         }
         const int jb = b & 3;
         tacc.x = jb == 0 ? word : tacc.x;
@@ -358,6 +375,8 @@ struct WideSmem {
 };
 
 // 128 threads (4 warps), thread t = slot t.  Called by all 128 threads of a block.
+// Same pipelining as fill_warp; the exchange goes through shared memory with one
+// barrier per band.
 template <bool kScores>
 __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, int t) {
     const CellConsts cc = make_consts(r, a.g);
@@ -374,7 +393,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     // bands 0 and 1 (trace tile 0: band 1, slot 127 = FROM_U)
     float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // my slot, band 1
     float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
-    int et = e0 - ((t - k0) & 127);                      // my event under band 1's placement
+    int ep = e0 - ((t - k0) & 127);                      // my event under band 1's placement
     ws.sc[1][t] = s_prev;
     ws.tile[0][t] = 0u;
     ws.tile[1][t] = 0u;
@@ -385,6 +404,8 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     }
     __syncthreads();
     if (t == 0) tile_bytes[(127 >> 2) * 16 + 1 * 4 + (127 & 3)] = (uint8_t)ABEA_FROM_U;
+    NextCell nc = next_cell(lp, ws.rg.ev[(ep + 1) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t], ws.rg.rsd[t],
+                            ws.rg.k1[t], cc);
     __syncthreads();
     unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
@@ -395,12 +416,12 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
         const float ll = ws.sc[pb][k0 & 127];
         const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
         const float left = ws.sc[pb][(t + 127) & 127];
-        // ---- phase A (previous placement only)
-        const float x = ws.rg.ev[(et + 1) & (kEvRing - 1)];
+        // ---- up candidate of band b
+        bool oku;
+        const float u = cell_u(s_prev, nc, cc, oku);
+        // ---- band b+1's emission side
         const float gmt = ws.rg.gm[t], sdt = ws.rg.sd[t], rst = ws.rg.rsd[t], k1t = ws.rg.k1[t];
-        float d, u, em;
-        bool okA;
-        cell_du(lp, s_prev, x, gmt, sdt, rst, k1t, cc, d, u, em, okA);
+        const NextCell nn = next_cell(left, ws.rg.ev[(ep + 2) & (kEvRing - 1)], gmt, sdt, rst, k1t, cc);
         // ---- placement
         const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
         k0 += right ? 1 : 0;
@@ -408,20 +429,20 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
         int lo, hi;
         band_range(k0, e0, n_events, n_kmers, lo, hi);
         const int o = (t - k0) & 127;
-        et = e0 - o;
+        ep = e0 - o;
         const bool valid = (o >= lo) && (o < hi);
-        // ---- phase B
+        // ---- skip candidate, comparison, tiers
         uint32_t from;
         bool need_l;
-        float best = cell_b(d, u, left, cc, from, need_l);
-        bool bad = valid && !okA;
+        float best = cell_b(nc.d, u, left, cc, from, need_l);
+        bool bad = valid && !(nc.ok && oku);
         if (need_l && valid) {
             bool ok;
-            best = cell_l(d, u, left, cc, from, ok);
+            best = cell_l(nc.d, u, left, cc, from, ok);
             bad |= !ok;
         }
         if (bad) {
-            best = cell_slow(lp, s_prev, left, x, gmt, sdt, k1t, cc, from);
+            best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], gmt, sdt, k1t, cc, from);
             ++slow;
         }
         best = valid ? best : -INFINITY;
@@ -442,12 +463,13 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
         }
         lp = left;
         s_prev = best;
+        nc = nn;
         ws.sc[b & 1][t] = best;
         tile_bytes[((b >> 2) & 1) * 512 + (t >> 2) * 16 + (b & 3) * 4 + (t & 3)] = (uint8_t)from;
         if (kScores) scores[(int64_t)b * kSlots + t] = best;
         if ((b & 127) == t) ws.k0s[t] = k0;
         // data for the next bands: wait before the barrier so it is visible after it
-        if ((b & 3) == 3) rings_step(ws.rg, rs, a, r, t, k0, e0, 5);
+        if ((b & 3) == 3) rings_step(ws.rg, rs, a, r, t, k0, e0, 7);
         __syncthreads();
         if ((b & 3) == 3 || b == n_bands - 1) {  // flush the finished tile, clear it for reuse
             uint32_t* tw = &ws.tile[(b >> 2) & 1][0];
