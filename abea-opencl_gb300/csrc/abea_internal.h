@@ -11,8 +11,9 @@
 //                       k-mer position (pre)
 //   last_col            f32 [per read: round_up(n_events,16)]   scores of the last
 //                       k-mer column, -inf where the cell was not computed (core)
-//   trace               u8  [per read: round_up(n_bands,4) * 128]  backpointers,
-//                       tiles of 4 bands x 128 k-mer slots (see trace_index)
+//   trace               u8  [per read: round_up(n_bands,4) * 128]  backpointers in
+//                       tiles of 4 bands x 128 k-mer slots, slot-major: one 32-bit
+//                       word per slot holds its 4 bands (see trace_index)
 //   scores              f32 [per read: round_up(n_bands,4) * 128]  optional, band-major, slot order
 //   band_k0             i32 [per read: round_up(n_bands,4)]        kmer_idx of each band's
 //                       lower-left cell (EventKmerPair.kmer_idx; event_idx = band-2-kmer_idx)
@@ -71,7 +72,7 @@ enum ReadStatus : int32_t {
 
 // Byte index of cell (band, slot) inside a read's trace region.
 __host__ __device__ inline int64_t trace_index(int64_t band, int slot) {
-    return (band >> 2) * 512 + (int64_t)(slot >> 2) * 16 + (band & 3) * 4 + (slot & 3);
+    return (band >> 2) * 512 + (int64_t)slot * 4 + (band & 3);
 }
 
 inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }

@@ -202,6 +202,16 @@ __device__ __forceinline__ void band_range(int k0, int e0, int n_events, int n_k
 // are computed during band b, before band b's own placement is decided.  Band b
 // itself then only needs its up candidate (from the slot's own previous score),
 // the exchange of neighbour cells, the skip candidate and the comparison.
+
+// 4x4 byte transpose: w[j] holds band j's backpointers of slots 0..3 (byte s);
+// returns o[s] holding slot s's backpointers of bands 0..3 (byte j).
+__device__ __forceinline__ uint4 transpose_bytes(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
+    const uint32_t a = __byte_perm(w0, w1, 0x5140), c = __byte_perm(w2, w3, 0x5140);
+    const uint32_t b = __byte_perm(w0, w1, 0x7362), d = __byte_perm(w2, w3, 0x7362);
+    return make_uint4(__byte_perm(a, c, 0x5410), __byte_perm(a, c, 0x7632), __byte_perm(b, d, 0x5410),
+                      __byte_perm(b, d, 0x7632));
+}
+
 template <bool kScores>
 __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int lane) {
     const CellConsts cc = make_consts(r, a.g);
@@ -248,7 +258,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
     int my_k0 = k0;  // bands 0 and 1 (lanes 0, 1) both have k0 = -51
     unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
-    uint4 tacc = make_uint4(0u, lane == 31 ? (ABEA_FROM_U << 24) : 0u, 0u, 0u);
+    uint32_t tw0 = 0u, tw1 = lane == 31 ? (ABEA_FROM_U << 24) : 0u, tw2 = 0u, tw3 = 0u;
 
     for (int b = 2; b < n_bands; ++b) {
         if ((b & 3) == 0) {
@@ -282,11 +292,11 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         e0 += right ? 0 : 1;
         int lo, hi;
         band_range(k0, e0, n_events, n_kmers, lo, hi);
-        // ---- skip candidate, comparison, tiers
+        // ---- skip candidate, comparison; rare tiers in one branch
         float best[4];
         uint32_t from[4];
         bool valid[4], need_l[4], bad[4];
-        bool any_l = false, any_bad = false;
+        bool rare = false;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int o = (4 * lane + j - k0) & 127;
@@ -295,27 +305,22 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
             best[j] = cell_b(nc[j].d, u[j], left[j], cc, from[j], need_l[j]);
             need_l[j] = need_l[j] && valid[j];
             bad[j] = valid[j] && !(nc[j].ok && oku[j]);
-            any_l |= need_l[j];
+            rare |= need_l[j] || bad[j];
         }
-        if (__any_sync(kFull, any_l)) {
+        if (__any_sync(kFull, rare)) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+            for (int j = 0; j < 4; ++j) {
                 if (need_l[j]) {
                     bool ok;
                     best[j] = cell_l(nc[j].d, u[j], left[j], cc, from[j], ok);
                     bad[j] |= !ok;
                 }
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) any_bad |= bad[j];
-        if (__any_sync(kFull, any_bad)) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
                 if (bad[j]) {
                     const float x = rg.ev[ep[j] & (kEvRing - 1)];
                     best[j] = cell_slow(LP[j], S1[j], left[j], x, gmv[j], sdv[j], k1v[j], cc, from[j]);
                     ++slow;
                 }
+            }
         }
         uint32_t word = 0;
 #pragma unroll
@@ -323,21 +328,17 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
             best[j] = valid[j] ? best[j] : -INFINITY;
             word |= (valid[j] ? from[j] : 0u) << (8 * j);
         }
-        // trim cell (k = -1, slot 127), GPU/align_cuda.cl:431-443
-        if (k0 <= -1 && k0 >= -kBand) {
-            if (lane == 31) {
+        // edges of the read: trim cell (k = -1, slot 127; GPU/align_cuda.cl:431-443)
+        // and the last k-mer column read by the post stage (GPU/align_cuda.cl:722-746)
+        const int ol = n_kmers - 1 - k0;
+        if (k0 <= -1 || ol < kBand) {
+            if (k0 <= -1 && k0 >= -kBand && lane == 31) {
                 const int e_t = e0 + 1 + k0;
                 const bool in = e_t >= 0 && e_t < n_events;
                 best[3] = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
                 word = (word & 0x00ffffffu) | (in ? (ABEA_FROM_U << 24) : 0u);
             }
-        }
-        // last k-mer column, consumed by the post stage (GPU/align_cuda.cl:722-746)
-        {
-            const int ol = n_kmers - 1 - k0;
-            if (ol >= lo && ol < hi) {
-                if (lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
-            }
+            if (ol >= lo && ol < hi && lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -346,17 +347,17 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
             nc[j] = nn[j];
         }
         const int jb = b & 3;
-        tacc.x = jb == 0 ? word : tacc.x;
-        tacc.y = jb == 1 ? word : tacc.y;
-        tacc.z = jb == 2 ? word : tacc.z;
-        tacc.w = jb == 3 ? word : tacc.w;
+        tw0 = jb == 0 ? word : tw0;
+        tw1 = jb == 1 ? word : tw1;
+        tw2 = jb == 2 ? word : tw2;
+        tw3 = jb == 3 ? word : tw3;
         if (jb == 3 || b == n_bands - 1) {
-            reinterpret_cast<uint4*>(trace + (int64_t)(b >> 2) * 512)[lane] = tacc;
-            tacc = make_uint4(0u, 0u, 0u, 0u);
+            reinterpret_cast<uint4*>(trace + (int64_t)(b >> 2) * 512)[lane] = transpose_bytes(tw0, tw1, tw2, tw3);
+            tw0 = tw1 = tw2 = tw3 = 0u;
         }
         if (kScores)
             reinterpret_cast<float4*>(scores + (int64_t)b * kSlots)[lane] = make_float4(best[0], best[1], best[2], best[3]);
-        if ((b & 31) == lane) my_k0 = k0;
+        my_k0 = ((b & 31) == lane) ? k0 : my_k0;
         if ((b & 31) == 31 || b == n_bands - 1) {
             if (lane <= (b & 31)) bk0[(b & ~31) + lane] = my_k0;
         }
@@ -369,9 +370,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 // ---------------------------------------------------------------- wide shape
 struct WideSmem {
     Rings rg;
-    float sc[2][kSlots];       // band scores by slot, double buffered
-    uint32_t tile[2][kSlots];  // trace tiles (4 bands x 128 slots = 512 B), double buffered
-    int32_t k0s[kSlots];       // band_k0 staging, 128 bands
+    float sc[2][kSlots];  // band scores by slot, double buffered
 };
 
 // 128 threads (4 warps), thread t = slot t.  Called by all 128 threads of a block.
@@ -385,28 +384,24 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
     int32_t* bk0 = a.band_k0 + r.band_off;
     float* lastc = a.last_col + r.ev_off;
-    uint8_t* tile_bytes = reinterpret_cast<uint8_t*>(&ws.tile[0][0]);
 
     int k0 = -1 - kBand / 2, e0 = kBand / 2;
     RingState rs;
     rings_init(ws.rg, rs, a, r, t, k0, e0);
-    // bands 0 and 1 (trace tile 0: band 1, slot 127 = FROM_U)
+    // bands 0 and 1: start cell and first trim cell in slot 127
     float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // my slot, band 1
     float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
     int ep = e0 - ((t - k0) & 127);                      // my event under band 1's placement
+    uint32_t tword = (t == 127) ? (ABEA_FROM_U << 8) : 0u;  // my backpointers of the current 4-band tile
+    int my_k0 = k0;
     ws.sc[1][t] = s_prev;
-    ws.tile[0][t] = 0u;
-    ws.tile[1][t] = 0u;
-    if (t == 0 || t == 1) ws.k0s[t] = k0;
     if (kScores) {
         scores[t] = (t == 127) ? 0.0f : -INFINITY;
         scores[kSlots + t] = s_prev;
     }
     __syncthreads();
-    if (t == 0) tile_bytes[(127 >> 2) * 16 + 1 * 4 + (127 & 3)] = (uint8_t)ABEA_FROM_U;
     NextCell nc = next_cell(lp, ws.rg.ev[(ep + 1) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t], ws.rg.rsd[t],
                             ws.rg.k1[t], cc);
-    __syncthreads();
     unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
 
@@ -431,54 +426,51 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
         const int o = (t - k0) & 127;
         ep = e0 - o;
         const bool valid = (o >= lo) && (o < hi);
-        // ---- skip candidate, comparison, tiers
+        // ---- skip candidate, comparison; rare tiers in one branch
         uint32_t from;
         bool need_l;
         float best = cell_b(nc.d, u, left, cc, from, need_l);
-        bool bad = valid && !(nc.ok && oku);
-        if (need_l && valid) {
-            bool ok;
-            best = cell_l(nc.d, u, left, cc, from, ok);
-            bad |= !ok;
-        }
-        if (bad) {
-            best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], gmt, sdt, k1t, cc, from);
-            ++slow;
+        bool bad = !(nc.ok && oku);
+        if (valid && (need_l || bad)) {
+            if (need_l) {
+                bool ok;
+                best = cell_l(nc.d, u, left, cc, from, ok);
+                bad |= !ok;
+            }
+            if (bad) {
+                best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], gmt, sdt, k1t, cc, from);
+                ++slow;
+            }
         }
         best = valid ? best : -INFINITY;
         from = valid ? from : 0u;
-        if (k0 <= -1 && k0 >= -kBand) {  // trim cell (k = -1, slot 127)
-            if (t == 127) {
+        const int ol = n_kmers - 1 - k0;
+        if (k0 <= -1 || ol < kBand) {  // trim cell (k = -1, slot 127); last k-mer column
+            if (t == 127 && k0 <= -1 && k0 >= -kBand) {
                 const int e_t = e0 + 1 + k0;
                 const bool in = e_t >= 0 && e_t < n_events;
                 best = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
                 from = in ? ABEA_FROM_U : 0u;
             }
-        }
-        {
-            const int ol = n_kmers - 1 - k0;
-            if (ol >= lo && ol < hi) {
-                if (t == sl_last) lastc[e0 - ol] = best;
-            }
+            if (t == sl_last && ol >= lo && ol < hi) lastc[e0 - ol] = best;
         }
         lp = left;
         s_prev = best;
         nc = nn;
         ws.sc[b & 1][t] = best;
-        tile_bytes[((b >> 2) & 1) * 512 + (t >> 2) * 16 + (b & 3) * 4 + (t & 3)] = (uint8_t)from;
+        tword |= from << (8 * (b & 3));
+        if ((b & 3) == 3 || b == n_bands - 1) {
+            reinterpret_cast<uint32_t*>(trace + (int64_t)(b >> 2) * 512)[t] = tword;
+            tword = 0u;
+        }
         if (kScores) scores[(int64_t)b * kSlots + t] = best;
-        if ((b & 127) == t) ws.k0s[t] = k0;
+        my_k0 = ((b & 127) == t) ? k0 : my_k0;
+        if ((b & 127) == 127 || b == n_bands - 1) {
+            if (t <= (b & 127)) bk0[(b & ~127) + t] = my_k0;
+        }
         // data for the next bands: wait before the barrier so it is visible after it
         if ((b & 3) == 3) rings_step(ws.rg, rs, a, r, t, k0, e0, 7);
         __syncthreads();
-        if ((b & 3) == 3 || b == n_bands - 1) {  // flush the finished tile, clear it for reuse
-            uint32_t* tw = &ws.tile[(b >> 2) & 1][0];
-            reinterpret_cast<uint32_t*>(trace + (int64_t)(b >> 2) * 512)[t] = tw[t];
-            tw[t] = 0u;  // next written two tiles later, after at least one more barrier
-        }
-        if ((b & 127) == 127 || b == n_bands - 1) {
-            if (t <= (b & 127)) bk0[(b & ~127) + t] = ws.k0s[t];
-        }
     }
     cp_async_wait_all();
     __syncthreads();
@@ -603,7 +595,7 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
                     ++n_out;
                     last_k = cur_k;
                     const int slot = cur_k & 127;
-                    const uint32_t from = tb[((lb >> 2) << 9) | ((slot >> 2) << 4) | ((lb & 3) << 2) | (slot & 3)];
+                    const uint32_t from = tb[((lb >> 2) << 9) | (slot << 2) | (lb & 3)];
                     step_back(from, cur_k, cur_e, gap, max_gap);
                 }
             }
