@@ -473,7 +473,7 @@ static int choose_wide_reads(const abea_batch* b, int sm_count, int64_t threshol
     const int blocks = batched_blocks_per_sm(scores) * sm_count;
     int64_t total = 0;
     for (const ReadDesc& r : b->reads) total += r.n_bands;
-    if (threshold <= 0) threshold = std::max<int64_t>(1, total / std::max(1, blocks * 4));
+    if (threshold <= 0) threshold = std::max<int64_t>(1, total / std::max(1, blocks * 8));
     int n = 0;
     for (int32_t i : b->order) {
         if (n >= blocks || b->reads[(size_t)i].n_bands < threshold) break;

@@ -368,113 +368,165 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 }
 
 // ---------------------------------------------------------------- wide shape
+// Eight warps per read.  Threads 0-127 ("band" threads) own slot t and run the
+// band-to-band critical path: up candidate, placement, skip candidate,
+// comparison, stores.  Threads 128-255 ("emission" threads) own slot t-128 and
+// compute, during band b, band b+1's emission and exact diagonal candidate,
+// handing them over in shared memory; they also run the prefetch rings.  One
+// barrier per band; every thread evaluates the band placement itself.
 struct WideSmem {
     Rings rg;
     float sc[2][kSlots];  // band scores by slot, double buffered
+    float nd[2][kSlots];  // next band: exact diagonal candidate
+    float np[2][kSlots];  // next band: em + stay split (p, w) for the up candidate
+    float nw[2][kSlots];
+    float ne[2][kSlots];  // next band: emission
+    int32_t nok[2][kSlots];
 };
 
-// 128 threads (4 warps), thread t = slot t.  Called by all 128 threads of a block.
-// Same pipelining as fill_warp; the exchange goes through shared memory with one
-// barrier per band.
+__device__ __forceinline__ void put_next(WideSmem& ws, int buf, int t, const NextCell& n) {
+    ws.nd[buf][t] = n.d;
+    ws.np[buf][t] = n.su.p;
+    ws.nw[buf][t] = n.su.w;
+    ws.ne[buf][t] = n.em;
+    ws.nok[buf][t] = n.ok ? 1 : 0;
+}
+
+__device__ __forceinline__ NextCell get_next(const WideSmem& ws, int buf, int t) {
+    NextCell n;
+    n.d = ws.nd[buf][t];
+    n.su.p = ws.np[buf][t];
+    n.su.w = ws.nw[buf][t];
+    n.em = ws.ne[buf][t];
+    n.ok = ws.nok[buf][t] != 0;
+    return n;
+}
+
+constexpr int kWideThreads = 256;
+
+// Named barrier 1 over the 256 threads of a wide read: the band and emission
+// threads reach it from different code paths, once per band each.
+__device__ __forceinline__ void wide_barrier() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+
+// Called by all 256 threads of a block.
 template <bool kScores>
-__device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, int t) {
+__device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, int tid) {
     const CellConsts cc = make_consts(r, a.g);
     const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
-    uint8_t* trace = a.trace + r.band_off * kSlots;
-    float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
-    int32_t* bk0 = a.band_k0 + r.band_off;
-    float* lastc = a.last_col + r.ev_off;
+    const bool band_thread = tid < kSlots;
+    const int t = tid & (kSlots - 1);
+    const int ring_t = band_thread ? 1000 : t;  // emission threads run the rings
 
     int k0 = -1 - kBand / 2, e0 = kBand / 2;
     RingState rs;
-    rings_init(ws.rg, rs, a, r, t, k0, e0);
-    // bands 0 and 1: start cell and first trim cell in slot 127
-    float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // my slot, band 1
-    float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
-    int ep = e0 - ((t - k0) & 127);                      // my event under band 1's placement
-    uint32_t tword = (t == 127) ? (ABEA_FROM_U << 8) : 0u;  // my backpointers of the current 4-band tile
-    int my_k0 = k0;
-    ws.sc[1][t] = s_prev;
-    if (kScores) {
-        scores[t] = (t == 127) ? 0.0f : -INFINITY;
-        scores[kSlots + t] = s_prev;
+    rings_init(ws.rg, rs, a, r, ring_t, k0, e0);
+    int ep = e0 - ((t - k0) & 127);  // my slot's event under the previous band's placement
+    if (band_thread) ws.sc[1][t] = (t == 127) ? a.g.trim_f : -INFINITY;
+    wide_barrier();
+    if (!band_thread) {
+        const float lp0 = (t == 0) ? 0.0f : -INFINITY;  // band 0 shifted by one slot
+        put_next(ws, 0, t, next_cell(lp0, ws.rg.ev[(ep + 1) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
+                                     ws.rg.rsd[t], ws.rg.k1[t], cc));
     }
-    __syncthreads();
-    NextCell nc = next_cell(lp, ws.rg.ev[(ep + 1) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t], ws.rg.rsd[t],
-                            ws.rg.k1[t], cc);
-    unsigned long long slow = 0;
-    const int sl_last = (n_kmers - 1) & 127;
-
-    for (int b = 2; b < n_bands; ++b) {
-        const int pb = (b - 1) & 1;
-        // ---- exchange (shared memory, written before the previous barrier)
-        const float ll = ws.sc[pb][k0 & 127];
-        const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
-        const float left = ws.sc[pb][(t + 127) & 127];
-        // ---- up candidate of band b
-        bool oku;
-        const float u = cell_u(s_prev, nc, cc, oku);
-        // ---- band b+1's emission side
-        const float gmt = ws.rg.gm[t], sdt = ws.rg.sd[t], rst = ws.rg.rsd[t], k1t = ws.rg.k1[t];
-        const NextCell nn = next_cell(left, ws.rg.ev[(ep + 2) & (kEvRing - 1)], gmt, sdt, rst, k1t, cc);
-        // ---- placement
-        const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
-        k0 += right ? 1 : 0;
-        e0 += right ? 0 : 1;
-        int lo, hi;
-        band_range(k0, e0, n_events, n_kmers, lo, hi);
-        const int o = (t - k0) & 127;
-        ep = e0 - o;
-        const bool valid = (o >= lo) && (o < hi);
-        // ---- skip candidate, comparison; rare tiers in one branch
-        uint32_t from;
-        bool need_l;
-        float best = cell_b(nc.d, u, left, cc, from, need_l);
-        bool bad = !(nc.ok && oku);
-        if (valid && (need_l || bad)) {
-            if (need_l) {
-                bool ok;
-                best = cell_l(nc.d, u, left, cc, from, ok);
-                bad |= !ok;
+    if (band_thread) {
+        // ------------------------------------------------ band threads
+        uint8_t* trace = a.trace + r.band_off * kSlots;
+        float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
+        int32_t* bk0 = a.band_k0 + r.band_off;
+        float* lastc = a.last_col + r.ev_off;
+        float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // band 1
+        float lp = (t == 0) ? 0.0f : -INFINITY;
+        uint32_t tword = (t == 127) ? (ABEA_FROM_U << 8) : 0u;
+        int my_k0 = k0;
+        if (kScores) {
+            scores[t] = (t == 127) ? 0.0f : -INFINITY;
+            scores[kSlots + t] = s_prev;
+        }
+        unsigned long long slow = 0;
+        const int sl_last = (n_kmers - 1) & 127;
+        wide_barrier();
+        for (int b = 2; b < n_bands; ++b) {
+            const int pb = (b - 1) & 1;
+            const float ll = ws.sc[pb][k0 & 127];
+            const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
+            const float left = ws.sc[pb][(t + 127) & 127];
+            const NextCell nc = get_next(ws, b & 1, t);
+            bool oku;
+            const float u = cell_u(s_prev, nc, cc, oku);
+            const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
+            k0 += right ? 1 : 0;
+            e0 += right ? 0 : 1;
+            int lo, hi;
+            band_range(k0, e0, n_events, n_kmers, lo, hi);
+            const int o = (t - k0) & 127;
+            ep = e0 - o;
+            const bool valid = (o >= lo) && (o < hi);
+            uint32_t from;
+            bool need_l;
+            float best = cell_b(nc.d, u, left, cc, from, need_l);
+            bool bad = !(nc.ok && oku);
+            if (valid && (need_l || bad)) {
+                if (need_l) {
+                    bool ok;
+                    best = cell_l(nc.d, u, left, cc, from, ok);
+                    bad |= !ok;
+                }
+                if (bad) {
+                    best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
+                                     ws.rg.k1[t], cc, from);
+                    ++slow;
+                }
             }
-            if (bad) {
-                best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], gmt, sdt, k1t, cc, from);
-                ++slow;
+            best = valid ? best : -INFINITY;
+            from = valid ? from : 0u;
+            const int ol = n_kmers - 1 - k0;
+            if (k0 <= -1 || ol < kBand) {  // trim cell (k = -1, slot 127); last k-mer column
+                if (t == 127 && k0 <= -1 && k0 >= -kBand) {
+                    const int e_t = e0 + 1 + k0;
+                    const bool in = e_t >= 0 && e_t < n_events;
+                    best = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
+                    from = in ? ABEA_FROM_U : 0u;
+                }
+                if (t == sl_last && ol >= lo && ol < hi) lastc[e0 - ol] = best;
             }
-        }
-        best = valid ? best : -INFINITY;
-        from = valid ? from : 0u;
-        const int ol = n_kmers - 1 - k0;
-        if (k0 <= -1 || ol < kBand) {  // trim cell (k = -1, slot 127); last k-mer column
-            if (t == 127 && k0 <= -1 && k0 >= -kBand) {
-                const int e_t = e0 + 1 + k0;
-                const bool in = e_t >= 0 && e_t < n_events;
-                best = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
-                from = in ? ABEA_FROM_U : 0u;
+            ws.sc[b & 1][t] = best;
+            lp = left;
+            s_prev = best;
+            tword |= from << (8 * (b & 3));
+            if ((b & 3) == 3 || b == n_bands - 1) {
+                reinterpret_cast<uint32_t*>(trace + (int64_t)(b >> 2) * 512)[t] = tword;
+                tword = 0u;
             }
-            if (t == sl_last && ol >= lo && ol < hi) lastc[e0 - ol] = best;
+            if (kScores) scores[(int64_t)b * kSlots + t] = best;
+            my_k0 = ((b & 127) == t) ? k0 : my_k0;
+            if ((b & 127) == 127 || b == n_bands - 1) {
+                if (t <= (b & 127)) bk0[(b & ~127) + t] = my_k0;
+            }
+            wide_barrier();
         }
-        lp = left;
-        s_prev = best;
-        nc = nn;
-        ws.sc[b & 1][t] = best;
-        tword |= from << (8 * (b & 3));
-        if ((b & 3) == 3 || b == n_bands - 1) {
-            reinterpret_cast<uint32_t*>(trace + (int64_t)(b >> 2) * 512)[t] = tword;
-            tword = 0u;
+        if (slow) atomicAdd(&a.counters[0], slow);
+    } else {
+        // ------------------------------------------------ emission threads
+        wide_barrier();
+        for (int b = 2; b < n_bands; ++b) {
+            const int pb = (b - 1) & 1;
+            const float ll = ws.sc[pb][k0 & 127];
+            const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
+            const float left = ws.sc[pb][(t + 127) & 127];
+            // band b+1: event two past the slot's event under band b-1's placement
+            const NextCell nn = next_cell(left, ws.rg.ev[(ep + 2) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
+                                          ws.rg.rsd[t], ws.rg.k1[t], cc);
+            put_next(ws, (b + 1) & 1, t, nn);
+            const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
+            k0 += right ? 1 : 0;
+            e0 += right ? 0 : 1;
+            ep = e0 - ((t - k0) & 127);
+            if ((b & 3) == 3) rings_step(ws.rg, rs, a, r, ring_t, k0, e0, 7);
+            wide_barrier();
         }
-        if (kScores) scores[(int64_t)b * kSlots + t] = best;
-        my_k0 = ((b & 127) == t) ? k0 : my_k0;
-        if ((b & 127) == 127 || b == n_bands - 1) {
-            if (t <= (b & 127)) bk0[(b & ~127) + t] = my_k0;
-        }
-        // data for the next bands: wait before the barrier so it is visible after it
-        if ((b & 3) == 3) rings_step(ws.rg, rs, a, r, t, k0, e0, 7);
-        __syncthreads();
     }
     cp_async_wait_all();
-    __syncthreads();
-    if (slow) atomicAdd(&a.counters[0], slow);
+    wide_barrier();
 }
 
 // ---------------------------------------------------------------- post
@@ -721,15 +773,17 @@ __global__ void __launch_bounds__(32) abea_post_kernel(PostArgs a) {
 }
 
 // ---------------------------------------------------------------- batched form
+constexpr int kBatchedWarps = kWideThreads / 32;
+
 struct BatchedSmem {
-    WideSmem wide;        // phase 1: the block's wide read
-    Rings warp_rings[4];  // phase 2: one per warp
-    PostSmem post[4];     // every warp's post staging
+    WideSmem wide;                     // phase 1: the block's wide read
+    Rings warp_rings[kBatchedWarps];   // phase 2: one per warp
+    PostSmem post[kBatchedWarps];      // every warp's post staging
     int32_t pick;
 };
 
 template <bool kScores>
-__global__ void __launch_bounds__(128) abea_batched_kernel(CoreArgs a, PostArgs p) {
+__global__ void __launch_bounds__(kWideThreads) abea_batched_kernel(CoreArgs a, PostArgs p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchedSmem& sm = *reinterpret_cast<BatchedSmem*>(smem_raw);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -785,10 +839,10 @@ int batched_blocks_per_sm(bool scores) {
         const size_t smem = sizeof(BatchedSmem);
         if (scores) {
             cudaFuncSetAttribute(abea_batched_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, abea_batched_kernel<true>, 128, smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, abea_batched_kernel<true>, kWideThreads, smem);
         } else {
             cudaFuncSetAttribute(abea_batched_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, abea_batched_kernel<false>, 128, smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, abea_batched_kernel<false>, kWideThreads, smem);
         }
         if (c <= 0) c = 1;
     }
@@ -801,13 +855,13 @@ cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
     cudaEventRecord(la.ev_pre, la.stream);
     const bool scores = la.core.scores != nullptr;
     const int max_blocks = batched_blocks_per_sm(scores) * la.sm_count;
-    const int want = la.core.n_wide + (n - la.core.n_wide + 3) / 4;
+    const int want = la.core.n_wide + (n - la.core.n_wide + kBatchedWarps - 1) / kBatchedWarps;
     const int grid = std::max(1, std::min(max_blocks, want));
     const size_t smem = sizeof(BatchedSmem);
     if (scores)
-        abea_batched_kernel<true><<<grid, 128, smem, la.stream>>>(la.core, la.post);
+        abea_batched_kernel<true><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
     else
-        abea_batched_kernel<false><<<grid, 128, smem, la.stream>>>(la.core, la.post);
+        abea_batched_kernel<false><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
     cudaEventRecord(la.ev_core, la.stream);
     *launches = 2;
     return cudaGetLastError();
