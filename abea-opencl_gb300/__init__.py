@@ -42,7 +42,7 @@ EXPORTS = [
     "abea_batch_results", "abea_batch_timing", "abea_batch_destroy", "abea_batch_read_bands",
     "abea_batch_best_scores", "abea_batch_slow_cells", "abea_host_alloc", "abea_host_free",
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
-    "abea_ctx_flush_l2", "abea_selftest_arith",
+    "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc",
 ]
 
 

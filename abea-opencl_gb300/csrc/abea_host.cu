@@ -829,3 +829,39 @@ extern "C" abea_status_t abea_ctx_flush_l2(abea_ctx_t* c) {
     CUDA_TRY(cudaMemsetAsync(c->flush_buf, (flip++) & 0xff, c->flush_bytes, c->stream));
     return ABEA_OK;
 }
+
+// ---------------------------------------------------------------- single-read description
+// ReadDesc of one read whose scratch regions all start at offset 0 (used by the
+// no-allocation entry point, which lays the regions out itself).
+namespace abea {
+ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scalings_t sc, int32_t out_capacity,
+                              int nonpos) {
+    ReadDesc r{};
+    const int32_t nk = sequence_len - ABEA_KMER_SIZE + 1;
+    r.n_events = n_events;
+    r.n_kmers = nk;
+    r.out_cap = out_capacity;
+    r.scale = sc.scale;
+    r.shift = sc.shift;
+    r.var = sc.var;
+    r.log_var = sc.log_var;
+    r.skip = (nk <= 0 || n_events <= 0) ? 1 : 0;
+    if (r.skip) return r;
+    r.n_bands = n_events + nk + 2;
+    Penalties p = penalties(n_events, nk);
+    r.lp_step = p.lp_step;
+    r.lp_stay = p.lp_stay;
+    split(p.lp_step, r.step_h, r.step_l);
+    split(p.lp_stay, r.stay_h, r.stay_l);
+    r.b_max = std::max(fabsf(r.step_h), fabsf(r.stay_h));
+    r.em_floor = pow2_floor(r.b_max);
+    r.nonpos = nonpos;
+    return r;
+}
+GlobalConsts parity_consts() { return global_consts(0); }
+}  // namespace abea
+
+extern "C" const char* abea_internal_set_error(const char* msg) {
+    g_last_error = msg;
+    return g_last_error.c_str();
+}

@@ -25,7 +25,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <stdio.h>
+
 #include <algorithm>
+#include <mutex>
 
 #include "abea_cell.cuh"
 #include "abea_internal.h"
@@ -868,3 +871,130 @@ cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
 }
 
 }  // namespace abea
+
+// ---------------------------------------------------------------- no-allocation entry point
+// For callers that cannot allocate device memory: a framework whose own
+// allocator owns the whole device and hands out every buffer, or a service whose
+// device memory budget is fixed when it starts.  One read goes through the plain
+// pre/core/post kernels with every scratch buffer carved out of one file-scope
+// device array, which exists on every GPU that loads this library for the life
+// of the process.  Calls whose work overlaps on the GPU race on that array.
+namespace abea {
+
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;  // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+__global__ void noalloc_write_desc(ReadDesc* dst, ReadDesc d) { *dst = d; }
+
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[256];  // device address of g_noalloc_scratch, per device
+
+static size_t noalloc_align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Bytes of scratch one read needs.
+static size_t noalloc_bytes(int32_t sequence_len, int32_t n_events) {
+    const int64_t nk = std::max<int64_t>(sequence_len - ABEA_KMER_SIZE + 1, 0);
+    const int64_t ne = std::max<int64_t>(n_events, 0);
+    const int64_t nb = (nk > 0 && ne > 0) ? ne + nk + 2 : 0;
+    const size_t ne_pad = (size_t)round_up(std::max<int64_t>(ne, 1), kChunk);
+    const size_t nk_pad = (size_t)round_up(std::max<int64_t>(nk, 1), kChunk);
+    const size_t nb_pad = (size_t)round_up(std::max<int64_t>(nb, 4), 4);
+    return noalloc_align(sizeof(ReadDesc)) + 2 * noalloc_align(4 * ne_pad) + 4 * noalloc_align(4 * nk_pad) +
+           noalloc_align(nb_pad * kSlots) + noalloc_align(4 * nb_pad) + noalloc_align(16) + noalloc_align(32);
+}
+
+}  // namespace abea
+
+extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t* n_pairs, int32_t out_capacity,
+                                            const char* sequence, int32_t sequence_len, const abea_event_t* events,
+                                            int32_t n_events, const abea_model_t* model, abea_scalings_t scaling,
+                                            void* stream) {
+    using namespace abea;
+    if (!pairs || !n_pairs || !sequence || !model || out_capacity < 0 || sequence_len < 0 || n_events < 0 ||
+        (n_events > 0 && !events)) {
+        abea_internal_set_error("abea_align_noalloc: invalid argument");
+        return ABEA_ERR_INVALID_ARG;
+    }
+    const size_t need = noalloc_bytes(sequence_len, n_events);
+    if (need > kNoAllocScratchBytes) {
+        char msg[256];
+        snprintf(msg, sizeof(msg),
+                 "abea_align_noalloc: the read needs %zu bytes of scratch but the fixed scratch holds %zu "
+                 "bytes (reads of up to about 250,000 bands, n_events + n_kmers + 2)",
+                 need, kNoAllocScratchBytes);
+        abea_internal_set_error(msg);
+        return ABEA_ERR_INVALID_ARG;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+        abea_internal_set_error("abea_align_noalloc: no current CUDA device");
+        return ABEA_ERR_NO_DEVICE;
+    }
+    unsigned char* base = nullptr;
+    {
+        // once per device, with that device current: the array's device address
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                char msg[256];
+                snprintf(msg, sizeof(msg), "abea_align_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+                abea_internal_set_error(msg);
+                return ABEA_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        base = (unsigned char*)g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int32_t nk = sequence_len - ABEA_KMER_SIZE + 1;
+    const int64_t nb = (nk > 0 && n_events > 0) ? (int64_t)n_events + nk + 2 : 0;
+    const size_t ne_pad = (size_t)round_up(std::max<int64_t>(n_events, 1), kChunk);
+    const size_t nk_pad = (size_t)round_up(std::max<int64_t>(nk, 1), kChunk);
+    const size_t nb_pad = (size_t)round_up(std::max<int64_t>(nb, 4), 4);
+    unsigned char* p = base;
+    auto carve = [&](size_t bytes) {
+        unsigned char* q = p;
+        p += noalloc_align(bytes);
+        return q;
+    };
+    ReadDesc* d_desc = (ReadDesc*)carve(sizeof(ReadDesc));
+    float* ev_mean = (float*)carve(4 * ne_pad);
+    float* last_col = (float*)carve(4 * ne_pad);
+    float* km_gm = (float*)carve(4 * nk_pad);
+    float* km_sd = (float*)carve(4 * nk_pad);
+    float* km_rsd = (float*)carve(4 * nk_pad);
+    float* km_k1 = (float*)carve(4 * nk_pad);
+    uint8_t* trace = (uint8_t*)carve(nb_pad * kSlots);
+    int32_t* band_k0 = (int32_t*)carve(4 * nb_pad);
+    float* best = (float*)carve(4);
+    int32_t* status = (int32_t*)(best + 1);
+    unsigned long long* counters = (unsigned long long*)carve(32);
+
+    // The pore model is not read on the host (it is device memory), so the
+    // kernels take the exact skip-candidate path for every cell (nonpos = 0).
+    const ReadDesc desc = describe_single_read(sequence_len, n_events, scaling, out_capacity, 0);
+    const GlobalConsts g = parity_consts();
+    // every call shares the array: clear what must start at zero
+    if (cudaMemsetAsync(counters, 0, 32, st) != cudaSuccess) {
+        abea_internal_set_error("abea_align_noalloc: cudaMemsetAsync failed");
+        return ABEA_ERR_CUDA;
+    }
+    noalloc_write_desc<<<1, 1, 0, st>>>(d_desc, desc);
+    PreArgs pre{d_desc, 1, g, sequence, events, model, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col};
+    CoreArgs core{d_desc, 1, g, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col, trace, nullptr, band_k0,
+                  counters, nullptr, nullptr, 0};
+    PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, last_col, trace, band_k0, pairs, n_pairs, best, status};
+    abea_pre_kernel<<<1, 128, 0, st>>>(pre);
+    abea_core_warp_kernel<false><<<1, 32, 0, st>>>(core);
+    abea_post_kernel<<<1, 32, 0, st>>>(post);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        char msg[256];
+        snprintf(msg, sizeof(msg), "abea_align_noalloc: launch failed: %s", cudaGetErrorString(e));
+        abea_internal_set_error(msg);
+        return ABEA_ERR_CUDA;
+    }
+    return ABEA_OK;
+}

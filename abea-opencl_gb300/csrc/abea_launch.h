@@ -7,6 +7,8 @@
 
 #include "abea_internal.h"
 
+extern "C" const char* abea_internal_set_error(const char* msg);
+
 namespace abea {
 
 struct PreArgs {
@@ -76,5 +78,10 @@ cudaError_t launch_plain(const LaunchArgs& a, int* launches);
 cudaError_t launch_batched(const LaunchArgs& a, int* launches);
 // Resident blocks per SM of the batched kernel.
 int batched_blocks_per_sm(bool scores);
+
+// Per-read constants of one read laid out at offset 0 of every scratch region.
+ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scalings_t sc, int32_t out_capacity,
+                              int nonpos);
+GlobalConsts parity_consts();
 
 }  // namespace abea

@@ -226,6 +226,28 @@ abea_status_t abea_ctx_flush_l2(abea_ctx_t *ctx);
  * "wrong" must be 0; "declined" cases take the FP64 path in the kernels. */
 abea_status_t abea_selftest_arith(int64_t cases, uint64_t seed, int64_t *out);
 
+/* ---- no-allocation entry point ------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory themselves or through this library: a framework whose own allocator
+ * owns the whole device and hands out every buffer, or a service whose device
+ * memory budget is fixed when it starts.  Aligns one read with
+ * the plain pre/core/post kernels on `stream` (a cudaStream_t; NULL = default
+ * stream) and returns without waiting.  Inputs (sequence, events, model) and
+ * outputs (pairs, capacity out_capacity; *n_pairs = count, 0 = failed QC,
+ * negative = abea_status_t of the read) are caller-owned device-accessible
+ * memory.  All scratch comes from one fixed 32 MiB device array inside this
+ * library, present on every GPU that loads it until the process exits; reads
+ * needing more (about 250,000 bands, n_events + n_kmers + 2) are rejected with
+ * ABEA_ERR_INVALID_ARG.  No cudaMalloc or other allocation happens.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress),
+ * so make it before any stream capture.  Every call uses the same array: calls
+ * whose work overlaps on the GPU (other streams, other threads) race; order
+ * them on one stream. */
+abea_status_t abea_align_noalloc(abea_aligned_pair_t *pairs, int32_t *n_pairs, int32_t out_capacity,
+                                 const char *sequence, int32_t sequence_len, const abea_event_t *events,
+                                 int32_t n_events, const abea_model_t *model, abea_scalings_t scaling,
+                                 void *stream);
+
 #ifdef __cplusplus
 }
 #endif
