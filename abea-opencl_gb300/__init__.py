@@ -42,7 +42,7 @@ EXPORTS = [
     "abea_batch_results", "abea_batch_timing", "abea_batch_destroy", "abea_batch_read_bands",
     "abea_batch_best_scores", "abea_batch_slow_cells", "abea_host_alloc", "abea_host_free",
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
-    "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc",
+    "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
 ]
 
 
@@ -121,6 +121,7 @@ def lib():
         L.abea_ctx_elapsed.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_float)]
         L.abea_ctx_flush_l2.argtypes = [vp]
         L.abea_selftest_arith.argtypes = [i64, C.c_uint64, vp]
+        L.abea_autotune.argtypes = [vp, vp, C.POINTER(i64), C.POINTER(C.c_float)]
         _lib = L
     return _lib
 
@@ -183,6 +184,12 @@ class DeviceBatch:
         v = C.c_int64()
         _check(lib().abea_batch_slow_cells(self.ctx.h, self.h, C.byref(v)))
         return v.value
+
+    def autotune(self):
+        """Picks the wide-shape threshold for this workload (abea_autotune)."""
+        thr, ms = C.c_int64(), C.c_float()
+        _check(lib().abea_autotune(self.ctx.h, self.h, C.byref(thr), C.byref(ms)))
+        return thr.value, ms.value
 
     def io_bytes(self):
         h2d, d2h, cells = C.c_int64(), C.c_int64(), C.c_int64()

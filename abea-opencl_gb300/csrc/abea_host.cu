@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 #include <new>
 #include <numeric>
@@ -102,8 +103,8 @@ struct abea_batch {
     bool scores_kept = false;
     bool ran = false;
     abea_timing_t timing{};
-    cudaGraphExec_t graph = nullptr;
-    int graph_mode = -1;
+    cudaGraphExec_t graph = nullptr;  // batched form: memsets + pre + fused core/post
+    uint64_t graph_key[4] = {0, 0, 0, 0};
 };
 
 struct abea_ctx {
@@ -120,6 +121,7 @@ struct abea_ctx {
     void* flush_buf = nullptr;
     size_t flush_bytes = 0;
     abea_batch* scratch = nullptr;  // reused by abea_align_batch / abea_align
+    std::map<uint64_t, int64_t> tuned;  // autotuned wide-shape threshold per workload signature
 };
 
 // ---------------------------------------------------------------- context
@@ -483,7 +485,7 @@ static int choose_wide_reads(const abea_batch* b, int sm_count, int64_t threshol
 }
 
 // Queues pre, core and post for a batch on the context's stream.
-static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches) {
+static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool capturing) {
     LaunchArgs la;
     const GlobalConsts g = global_consts(0);
     la.pre = PreArgs{b->d_reads, b->n_reads, g, b->d_seq, b->d_ev, b->d_model, b->d_ev_mean, b->d_km_gm,
@@ -498,9 +500,30 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches) {
     la.stream = c->stream;
     la.ev_pre = c->ev[1];
     la.ev_core = c->ev[2];
+    la.capturing = capturing;
     cudaError_t e = c->mode == ABEA_MODE_BATCHED ? launch_batched(la, launches) : launch_plain(la, launches);
     if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
     return ABEA_OK;
+}
+
+static abea_status_t collect_timing(abea_ctx* c, abea_batch* b);
+
+// Workload signature for the autotuner: log2 buckets of the longest read's bands,
+// of the read count and of the total bands.
+static uint64_t workload_signature(const abea_batch* b) {
+    int64_t mx = 0, tot = 0;
+    for (const ReadDesc& r : b->reads) {
+        mx = std::max<int64_t>(mx, r.n_bands);
+        tot += r.n_bands;
+    }
+    auto lg = [](int64_t v) { int k = 0; while (v > 1) { v >>= 1; ++k; } return (uint64_t)k; };
+    return (lg(mx) << 16) | (lg(b->n_reads) << 8) | lg(tot);
+}
+
+static abea_status_t queue_work(abea_ctx* c, abea_batch* b, int* launches, bool capturing) {
+    CUDA_TRY(cudaMemsetAsync(b->d_slow, 0, sizeof(unsigned long long) * 4, c->stream));
+    CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int32_t) * 8, c->stream));
+    return launch_all(c, b, launches, capturing);
 }
 
 static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
@@ -512,17 +535,96 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
     }
     // wide shape for the longest reads in the batched form
     b->n_wide = 0;
-    if (c->mode == ABEA_MODE_BATCHED)
-        b->n_wide = choose_wide_reads(b, c->sm_count, c->long_read_bands, b->scores_kept);
-    CUDA_TRY(cudaMemsetAsync(b->d_slow, 0, sizeof(unsigned long long) * 4, c->stream));
-    CUDA_TRY(cudaMemsetAsync(b->d_queue, 0, sizeof(int32_t) * 8, c->stream));
-    CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
+    if (c->mode == ABEA_MODE_BATCHED) {
+        int64_t thr = c->long_read_bands;
+        if (thr == 0) {
+            auto it = c->tuned.find(workload_signature(b));
+            if (it != c->tuned.end()) thr = it->second;
+        }
+        b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept);
+    }
     int launches = 0;
-    abea_status_t st = launch_all(c, b, &launches);
-    if (st) return st;
-    CUDA_TRY(cudaEventRecord(c->ev[3], c->stream));
+    if (c->mode == ABEA_MODE_BATCHED && c->use_graph) {
+        // the whole run as one CUDA graph, re-captured when its parameters change
+        const uint64_t key[4] = {(uint64_t)(uintptr_t)b->slab.base, (uint64_t)b->n_reads, (uint64_t)b->n_wide,
+                                 (uint64_t)(b->scores_kept ? 1 : 0)};
+        if (!b->graph || memcmp(key, b->graph_key, sizeof(key)) != 0) {
+            if (b->graph) cudaGraphExecDestroy(b->graph);
+            b->graph = nullptr;
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            abea_status_t st = queue_work(c, b, &launches, true);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (st) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&b->graph, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                b->graph = nullptr;
+                return fail(ABEA_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+            }
+            memcpy(b->graph_key, key, sizeof(key));
+        }
+        launches = 2;
+        CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
+        CUDA_TRY(cudaGraphLaunch(b->graph, c->stream));
+        CUDA_TRY(cudaEventRecord(c->ev[3], c->stream));
+    } else {
+        CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
+        abea_status_t st = queue_work(c, b, &launches, false);
+        if (st) return st;
+        CUDA_TRY(cudaEventRecord(c->ev[3], c->stream));
+    }
     b->timing.kernel_launches = launches;
     b->ran = true;
+    return ABEA_OK;
+}
+
+// Autotuner: times the batched form on `b` with candidate thresholds for the
+// wide (256-thread) shape — none, the heuristic, the longest eighth / quarter /
+// half of the resident blocks, and every read that fits — keeps the fastest for
+// this workload signature (longest read, read count and total bands, log2
+// buckets) and returns it.
+extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* best_threshold, float* best_ms) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune: null argument");
+    if (b->n_reads == 0) return ABEA_OK;
+    const abea_mode_t mode0 = c->mode;
+    const int64_t thr0 = c->long_read_bands;
+    c->mode = ABEA_MODE_BATCHED;
+    const int blocks = batched_blocks_per_sm(b->scores_kept) * c->sm_count;
+    int64_t total = 0;
+    for (const ReadDesc& r : b->reads) total += r.n_bands;
+    std::vector<int64_t> cands = {INT64_MAX, std::max<int64_t>(1, total / std::max(1, blocks * 8))};
+    for (int div : {8, 4, 2, 1}) {
+        size_t k = std::min<size_t>(b->order.size(), (size_t)std::max(1, blocks / div)) - 1;
+        cands.push_back(std::max<int64_t>(1, b->reads[(size_t)b->order[k]].n_bands));
+    }
+    int64_t best = 0;
+    float best_t = 1e30f;
+    abea_status_t st = ABEA_OK;
+    for (int64_t cand : cands) {
+        c->long_read_bands = cand;
+        float t_min = 1e30f;
+        for (int rep = 0; rep < 3 && !st; ++rep) {
+            if ((st = run_batch(c, b))) break;
+            if ((st = collect_timing(c, b))) break;
+            if (rep > 0) t_min = std::min(t_min, b->timing.total_ms);
+        }
+        if (st) break;
+        if (t_min < best_t) {
+            best_t = t_min;
+            best = cand;
+        }
+    }
+    c->mode = mode0;
+    c->long_read_bands = thr0;
+    if (st) return st;
+    c->tuned[workload_signature(b)] = best;
+    if (best_threshold) *best_threshold = best;
+    if (best_ms) *best_ms = best_t;
     return ABEA_OK;
 }
 

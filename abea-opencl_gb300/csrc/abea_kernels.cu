@@ -639,19 +639,25 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
             if (next_lo >= 0) stage(next_lo, buf ^ 1);
             if (lane == 0) {
                 const uint8_t* tb = sm.tr[buf];
+                int lb = cur_e + cur_k + 2 - chunk_lo, slot = cur_k & 127;
                 while (true) {
-                    if (cur_k < 0 || cur_e < 0) {
+                    if ((cur_k | cur_e) < 0) {
                         done = true;
                         break;
                     }
-                    const int lb = cur_e + cur_k + 2 - chunk_lo;
                     if (lb < 0) break;
                     if (n_out < cap) out[n_out] = abea_aligned_pair_t{cur_k, cur_e};
                     ++n_out;
                     last_k = cur_k;
-                    const int slot = cur_k & 127;
                     const uint32_t from = tb[((lb >> 2) << 9) | (slot << 2) | (lb & 3)];
-                    step_back(from, cur_k, cur_e, gap, max_gap);
+                    // D: band-2, slot-1; U: band-1, same slot; L: band-1, slot-1
+                    const bool is_u = from == ABEA_FROM_U, is_l = from == ABEA_FROM_L;
+                    lb -= (is_u || is_l) ? 1 : 2;
+                    slot = is_u ? slot : ((slot - 1) & 127);
+                    cur_k -= is_u ? 0 : 1;
+                    cur_e -= is_l ? 0 : 1;
+                    gap = is_l ? gap + 1 : 0;
+                    max_gap = max(max_gap, gap);
                 }
             }
             done = __shfl_sync(kFull, (int)done, 0) != 0;
@@ -824,12 +830,12 @@ __global__ void __launch_bounds__(kWideThreads) abea_batched_kernel(CoreArgs a, 
 cudaError_t launch_plain(const LaunchArgs& la, int* launches) {
     const int n = la.core.n_reads;
     abea_pre_kernel<<<n, 128, 0, la.stream>>>(la.pre);
-    cudaEventRecord(la.ev_pre, la.stream);
+    cudaEventRecordWithFlags(la.ev_pre, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     if (la.core.scores)
         abea_core_warp_kernel<true><<<n, 32, 0, la.stream>>>(la.core);
     else
         abea_core_warp_kernel<false><<<n, 32, 0, la.stream>>>(la.core);
-    cudaEventRecord(la.ev_core, la.stream);
+    cudaEventRecordWithFlags(la.ev_core, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     abea_post_kernel<<<n, 32, 0, la.stream>>>(la.post);
     *launches = 3;
     return cudaGetLastError();
@@ -855,7 +861,7 @@ int batched_blocks_per_sm(bool scores) {
 cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
     const int n = la.core.n_reads;
     abea_pre_kernel<<<n, 128, 0, la.stream>>>(la.pre);
-    cudaEventRecord(la.ev_pre, la.stream);
+    cudaEventRecordWithFlags(la.ev_pre, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     const bool scores = la.core.scores != nullptr;
     const int max_blocks = batched_blocks_per_sm(scores) * la.sm_count;
     const int want = la.core.n_wide + (n - la.core.n_wide + kBatchedWarps - 1) / kBatchedWarps;
@@ -865,7 +871,7 @@ cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
         abea_batched_kernel<true><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
     else
         abea_batched_kernel<false><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
-    cudaEventRecord(la.ev_core, la.stream);
+    cudaEventRecordWithFlags(la.ev_core, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     *launches = 2;
     return cudaGetLastError();
 }

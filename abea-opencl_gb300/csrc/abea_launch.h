@@ -70,6 +70,7 @@ struct LaunchArgs {
     cudaStream_t stream;
     cudaEvent_t ev_pre;   // recorded after pre
     cudaEvent_t ev_core;  // recorded after core (batched: after the fused core+post)
+    bool capturing;       // the launches are being captured into a CUDA graph
 };
 
 // Plain form: pre, core, post — one block per read each, as the reference.

@@ -179,6 +179,13 @@ abea_status_t abea_batch_results(abea_ctx_t *ctx, abea_batch_t *batch,
 abea_status_t abea_batch_timing(abea_ctx_t *ctx, abea_batch_t *batch, abea_timing_t *timing);
 void abea_batch_destroy(abea_batch_t *batch);
 
+/* Autotuner: runs the batched form on `batch` with several thresholds for the
+ * wide (256-thread) shape and keeps the fastest for this workload's signature
+ * (log2 buckets of its longest read, read count and total bands); later
+ * batched runs with ABEA_OPT_LONG_READ_BANDS = 0 and the same signature use it.
+ * Returns the threshold (INT64_MAX = no wide reads) and its time. */
+abea_status_t abea_autotune(abea_ctx_t *ctx, abea_batch_t *batch, int64_t *best_threshold, float *best_ms);
+
 /* Band matrices of one read after a run, converted to the reference layout
  * (GPU/align_cuda.c:573-583): bands[n_bands*100] scores (needs
  * ABEA_OPT_STORE_SCORES=1, else NULL must be passed), trace[n_bands*100]
