@@ -85,18 +85,6 @@ class Dist:
             self.pg.destroy_process_group()
 
 
-def shard_reads(n_bands: np.ndarray, world: int, rank: int) -> np.ndarray:
-    """Longest-processing-time partition of reads over ranks by band cells."""
-    order = np.argsort(-n_bands, kind="stable")
-    load = np.zeros(world, dtype=np.int64)
-    owner = np.zeros(len(n_bands), dtype=np.int64)
-    for i in order:
-        r = int(np.argmin(load))
-        owner[i] = r
-        load[r] += int(n_bands[i])
-    return np.nonzero(owner == rank)[0]
-
-
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
@@ -259,9 +247,11 @@ def time_e2e(pkg, ctx, batch, steps: int, warmup: int):
             L.abea_host_free(p)
 
 
-def run_mode(pkg, batch, mode, device, steps, warmup):
+def run_mode(pkg, batch, mode, device, steps, warmup, autotune=False):
     ctx = pkg.Context(device, mode)
     dev = ctx.upload(batch)
+    if autotune and mode == pkg.MODE_BATCHED:
+        dev.autotune()
     per_step, core, timing = time_device(pkg, ctx, dev, steps, warmup)
     res = dict(per_step=per_step, core=core, timing=timing, slow=dev.slow_cells())
     dev.close()
@@ -273,6 +263,7 @@ def ours(args, dist):
     pkg = load_package()
     from abea_gb300 import synth
     device = dist.local_rank
+    from abea_gb300.shard import shard_reads
     full = synth.make_batch(args.workload, seed=args.seed)
     shard = shard_reads(full.n_bands(), dist.world, dist.rank) if dist.world > 1 else np.arange(full.n_reads)
     batch = full.subset(shard) if dist.world > 1 else full
@@ -281,6 +272,9 @@ def ours(args, dist):
 
     ctx = pkg.Context(device, mode)
     dev = ctx.upload(batch)
+    tuned = None
+    if mode == pkg.MODE_BATCHED and args.autotune:
+        tuned = dev.autotune()  # untimed: picks the wide-shape threshold for this workload
     launches_per_step = None
     for _ in range(args.warmup):
         dev.run()
@@ -327,6 +321,7 @@ def ours(args, dist):
         "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload),
                    "reads": int(total_reads), "band_cells": int(total_cells), "seed": args.seed,
                    "mode": args.mode, "parallelism": f"reads sharded over {dist.world} GPU(s)",
+                   "autotuned_wide_threshold_bands": None if tuned is None else tuned[0],
                    "l2": "flushed (write of 2x L2) before every timed step"},
         "reads_per_s": total_reads / (ms_per_step / 1e3),
         "gpu_launches": int(launches_per_step or 0) * args.steps,
@@ -359,7 +354,7 @@ def ours(args, dist):
         ub = synth.make_batch("uneven", seed=args.seed)
         un = {}
         for name, m in (("batched", pkg.MODE_BATCHED), ("plain", pkg.MODE_PLAIN)):
-            r = run_mode(pkg, ub, m, device, 2, 1)
+            r = run_mode(pkg, ub, m, device, 2, 1, autotune=args.autotune)
             ms = statistics.mean(r["per_step"])
             un[name] = {"value": ub.band_cells() / (ms / 1e3), "ms_per_step": ms}
         un["batched_over_plain"] = un["batched"]["value"] / un["plain"]["value"]
@@ -385,6 +380,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-compare", dest="compare", action="store_false")
     ap.add_argument("--no-cpu", dest="cpu", action="store_false")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     args = ap.parse_args()
     dist = Dist()
     try:

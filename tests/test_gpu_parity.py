@@ -192,3 +192,19 @@ def test_uneven_batch_batched_equals_plain(lib):
     _, p1, c1 = run(batch, abea.MODE_PLAIN)
     _, p2, c2 = run(batch, abea.MODE_BATCHED)
     assert_same_alignments(batch, p2, c2, p1, c1)
+
+
+def test_autotuned_batched_stays_exact(lib, oracle_mod):
+    """The autotuner only changes which reads run on the wide shape; results
+    stay bit-exact, through the CUDA-graph replay of the batched form."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("uneven", seed=5)
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    dev = ctx.upload(batch)
+    thr, ms = dev.autotune()
+    assert thr > 0 and ms > 0
+    dev.run()
+    gp, gc = dev.results()
+    assert dev.timing()["kernel_launches"] == 2  # pre + fused core/post, one graph
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
