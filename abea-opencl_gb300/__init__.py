@@ -29,7 +29,7 @@ LIB_PATH = os.path.join(HERE, "libabea.so")
 
 MODE_PLAIN = 0
 MODE_BATCHED = 1
-OPT_MODE, OPT_STORE_SCORES, OPT_USE_GRAPH, OPT_LONG_READ_BANDS, OPT_SPIN_LIMIT = range(5)
+OPT_MODE, OPT_STORE_SCORES, OPT_USE_GRAPH, OPT_LONG_READ_BANDS, OPT_SPIN_LIMIT, OPT_VAR_AWARE = range(6)
 
 STATUS = {
     0: "ok", -1: "invalid argument", -2: "capacity", -3: "out of memory", -4: "CUDA error",
@@ -43,6 +43,7 @@ EXPORTS = [
     "abea_batch_best_scores", "abea_batch_slow_cells", "abea_host_alloc", "abea_host_free",
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
     "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
+    "abea_batch_backward", "abea_batch_set_scalings", "abea_batch_recalibrate",
 ]
 
 
@@ -122,6 +123,9 @@ def lib():
         L.abea_ctx_flush_l2.argtypes = [vp]
         L.abea_selftest_arith.argtypes = [i64, C.c_uint64, vp]
         L.abea_autotune.argtypes = [vp, vp, C.POINTER(i64), C.POINTER(C.c_float)]
+        L.abea_batch_backward.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.abea_batch_set_scalings.argtypes = [vp, vp, vp]
+        L.abea_batch_recalibrate.argtypes = [vp, vp, i32, C.c_double, vp]
         _lib = L
     return _lib
 
@@ -190,6 +194,33 @@ class DeviceBatch:
         thr, ms = C.c_int64(), C.c_float()
         _check(lib().abea_autotune(self.ctx.h, self.h, C.byref(thr), C.byref(ms)))
         return thr.value, ms.value
+
+    def backward(self, model_grad: bool = True):
+        """Adjoint of the last run (abea_batch_backward): dict with grad_scalings
+        [n,3] (d/d shift, scale, var), grad_model [4096,2] (d/d level_mean,
+        level_stdv) or None, path_emission [n] and status [n]."""
+        n = self.batch.n_reads
+        g = np.zeros((max(n, 1), 3))
+        gm = np.zeros((4096, 2)) if model_grad else None
+        em = np.zeros(max(n, 1))
+        st = np.zeros(max(n, 1), dtype=np.int32)
+        _check(lib().abea_batch_backward(self.ctx.h, self.h, _p(g), _p(gm), _p(em), _p(st)))
+        return dict(grad_scalings=g[:n], grad_model=gm, path_emission=em[:n], status=st[:n])
+
+    def set_scalings(self, scalings):
+        sc = np.ascontiguousarray(scalings, dtype=SCALINGS_DTYPE)
+        if len(sc) != self.batch.n_reads:
+            raise ValueError("one scalings record per read")
+        _check(lib().abea_batch_set_scalings(self.ctx.h, self.h, _p(sc)))
+
+    def recalibrate(self, iterations: int = 3, first_temperature: float = 5.0):
+        """Annealed Gauss-Newton recalibration of (shift, scale)
+        (abea_batch_recalibrate); returns the final scalings, the batch left
+        aligned with them."""
+        out = np.zeros(max(self.batch.n_reads, 1), dtype=SCALINGS_DTYPE)
+        _check(lib().abea_batch_recalibrate(self.ctx.h, self.h, int(iterations), float(first_temperature),
+                                            _p(out)))
+        return out[: self.batch.n_reads]
 
     def io_bytes(self):
         h2d, d2h, cells = C.c_int64(), C.c_int64(), C.c_int64()

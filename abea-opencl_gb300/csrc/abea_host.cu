@@ -76,6 +76,8 @@ struct DevSlab {
 struct abea_batch {
     abea_ctx* ctx = nullptr;
     int32_t n_reads = 0;
+    int32_t var_aware = 0;       // emissions use var (ABEA_OPT_VAR_AWARE at creation)
+    float min_lsd = 0.0f;        // smallest cached log stdv of the model
     std::vector<ReadDesc> reads;
     std::vector<int32_t> order;  // longest first
     int32_t n_wide = 0;          // leading reads of `order` run on the wide shape
@@ -100,6 +102,9 @@ struct abea_batch {
     unsigned long long* d_slow = nullptr;
     int32_t* d_order = nullptr;
     int32_t* d_queue = nullptr;
+    // adjoint
+    int32_t *d_path_len = nullptr, *d_path_flags = nullptr, *d_best_event = nullptr, *d_adj_status = nullptr;
+    double *d_grad_sc = nullptr, *d_gn = nullptr, *d_path_em = nullptr, *d_grad_model = nullptr;
     bool scores_kept = false;
     bool ran = false;
     abea_timing_t timing{};
@@ -115,6 +120,7 @@ struct abea_ctx {
     int64_t use_graph = 1;
     int64_t long_read_bands = 0;
     int64_t spin_limit = 1 << 22;
+    int64_t var_aware = 0;
     int sm_count = 0;
     cudaEvent_t ev[8] = {};
     cudaEvent_t marker[16] = {};
@@ -200,6 +206,7 @@ extern "C" abea_status_t abea_ctx_set_option(abea_ctx_t* c, abea_option_t opt, i
         if (v <= 0) return fail(ABEA_ERR_INVALID_ARG, "spin limit must be positive");
         c->spin_limit = v;
         return ABEA_OK;
+    case ABEA_OPT_VAR_AWARE: c->var_aware = v != 0; return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -212,6 +219,7 @@ extern "C" abea_status_t abea_ctx_get_option(abea_ctx_t* c, abea_option_t opt, i
     case ABEA_OPT_USE_GRAPH: *v = c->use_graph; return ABEA_OK;
     case ABEA_OPT_LONG_READ_BANDS: *v = c->long_read_bands; return ABEA_OK;
     case ABEA_OPT_SPIN_LIMIT: *v = c->spin_limit; return ABEA_OK;
+    case ABEA_OPT_VAR_AWARE: *v = c->var_aware; return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -297,19 +305,30 @@ static abea_status_t validate(const HostInputs& in) {
 // 1 when log_inv_sqrt_2pi - log(stdv) <= 0 for every k-mer of the model (with
 // the read's log_var in var-aware mode): then every emission and every score of
 // the read is <= 0, which the kernels' fast tier relies on.
-static int model_nonpos(const abea_model_t* model, float log_var, int var_aware) {
+// Both roundings are monotone, so the largest K1 comes from the smallest cached
+// log stdv: the test runs on that one value per read.
+static float model_min_log_stdv(const abea_model_t* model) {
+    float m = INFINITY;
     for (int k = 0; k < ABEA_NUM_KMER; ++k) {
-        volatile float lsd = model[k].level_log_stdv;
-        if (var_aware) lsd = lsd + log_var;
-        volatile float k1 = -0.918938f - lsd;
-        if (!(k1 <= 0.0f)) return 0;
+        const float v = model[k].level_log_stdv;
+        if (v != v) return v;  // NaN: no read of the batch takes the shortcut
+        if (v < m) m = v;
     }
-    return 1;
+    return m;
 }
 
-static abea_status_t plan(abea_batch* b, const HostInputs& in) {
+static int model_nonpos(float min_lsd, float log_var, int var_aware) {
+    volatile float lsd = min_lsd;
+    if (var_aware) lsd = lsd + log_var;
+    volatile float k1 = -0.918938f - lsd;
+    return k1 <= 0.0f ? 1 : 0;
+}
+
+static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware) {
     b->n_reads = in.n_reads;
-    const int nonpos = in.n_reads > 0 ? model_nonpos(in.model, 0.0f, 0) : 1;
+    b->var_aware = var_aware;
+    const float min_lsd = in.n_reads > 0 ? model_min_log_stdv(in.model) : 0.0f;
+    b->min_lsd = min_lsd;
     b->reads.assign((size_t)in.n_reads, ReadDesc{});
     int64_t seq_end = 0, ev_end = 0, km = 0, ev = 0, bands = 0, cells = 0;
     for (int32_t i = 0; i < in.n_reads; ++i) {
@@ -344,7 +363,7 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in) {
         split(p.lp_stay, r.stay_h, r.stay_l);
         r.b_max = std::max(fabsf(r.step_h), fabsf(r.stay_h));
         r.em_floor = pow2_floor(r.b_max);
-        r.nonpos = nonpos;
+        r.nonpos = model_nonpos(min_lsd, r.log_var, var_aware);
         r.ev_off = ev;
         r.km_off = km;
         r.band_off = bands;
@@ -374,7 +393,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Carves the device slab; grows it when needed.
 static abea_status_t ensure_device(abea_batch* b, bool scores) {
     size_t n = (size_t)std::max(b->n_reads, 1);
-    size_t sizes[21] = {
+    size_t sizes[29] = {
         sizeof(ReadDesc) * n,                                   // reads
         (size_t)std::max<int64_t>(b->seq_bytes, 1),             // seq
         sizeof(abea_event_t) * (size_t)std::max<int64_t>(b->n_events_total, 1),
@@ -395,8 +414,16 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         sizeof(unsigned long long) * 4,  // slow counter
         sizeof(int32_t) * n,   // order
         sizeof(int32_t) * 8,   // queue counters
+        sizeof(int32_t) * n,   // path_len
+        sizeof(int32_t) * n,   // path_flags
+        sizeof(int32_t) * n,   // best_event
+        sizeof(int32_t) * n,   // adj_status
+        sizeof(double) * 3 * n,  // grad_sc
+        sizeof(double) * 5 * n,  // gn
+        sizeof(double) * n,      // path_em
+        sizeof(double) * 2 * ABEA_NUM_KMER,  // grad_model
         0};
-    const int n_bufs = 20;
+    const int n_bufs = 28;
     size_t total = 0;
     for (int i = 0; i < n_bufs; ++i) total += align256(sizes[i]);
     if (total > b->slab.bytes) {
@@ -412,7 +439,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         b->slab.bytes = total;
     }
     char* p = (char*)b->slab.base;
-    void* ptrs[21];
+    void* ptrs[29];
     for (int i = 0; i < n_bufs; ++i) {
         ptrs[i] = sizes[i] ? (void*)p : nullptr;
         p += align256(sizes[i]);
@@ -437,6 +464,14 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
     b->d_slow = (unsigned long long*)ptrs[17];
     b->d_order = (int32_t*)ptrs[18];
     b->d_queue = (int32_t*)ptrs[19];
+    b->d_path_len = (int32_t*)ptrs[20];
+    b->d_path_flags = (int32_t*)ptrs[21];
+    b->d_best_event = (int32_t*)ptrs[22];
+    b->d_adj_status = (int32_t*)ptrs[23];
+    b->d_grad_sc = (double*)ptrs[24];
+    b->d_gn = (double*)ptrs[25];
+    b->d_path_em = (double*)ptrs[26];
+    b->d_grad_model = (double*)ptrs[27];
     b->scores_kept = scores;
     return ABEA_OK;
 }
@@ -487,7 +522,7 @@ static int choose_wide_reads(const abea_batch* b, int sm_count, int64_t threshol
 // Queues pre, core and post for a batch on the context's stream.
 static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool capturing) {
     LaunchArgs la;
-    const GlobalConsts g = global_consts(0);
+    const GlobalConsts g = global_consts(b->var_aware);
     la.pre = PreArgs{b->d_reads, b->n_reads, g, b->d_seq, b->d_ev, b->d_model, b->d_ev_mean, b->d_km_gm,
                      b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col};
     la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
@@ -495,7 +530,7 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
                        b->d_slow, b->d_order, b->d_queue, b->n_wide};
     la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
-                       b->d_status};
+                       b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event};
     la.sm_count = c->sm_count;
     la.stream = c->stream;
     la.ev_pre = c->ev[1];
@@ -547,7 +582,7 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
     if (c->mode == ABEA_MODE_BATCHED && c->use_graph) {
         // the whole run as one CUDA graph, re-captured when its parameters change
         const uint64_t key[4] = {(uint64_t)(uintptr_t)b->slab.base, (uint64_t)b->n_reads, (uint64_t)b->n_wide,
-                                 (uint64_t)(b->scores_kept ? 1 : 0)};
+                                 (uint64_t)(b->scores_kept ? 1 : 0) | ((uint64_t)b->var_aware << 1)};
         if (!b->graph || memcmp(key, b->graph_key, sizeof(key)) != 0) {
             if (b->graph) cudaGraphExecDestroy(b->graph);
             b->graph = nullptr;
@@ -688,7 +723,7 @@ extern "C" abea_status_t abea_batch_create(abea_ctx_t* c, int32_t n_reads, const
     abea_batch* b = new (std::nothrow) abea_batch();
     if (!b) return fail(ABEA_ERR_OUT_OF_MEMORY, "host allocation failed");
     b->ctx = c;
-    if ((st = plan(b, in)) || (st = ensure_device(b, c->store_scores != 0)) || (st = upload(b, in, c->stream))) {
+    if ((st = plan(b, in, (int)c->var_aware)) || (st = ensure_device(b, c->store_scores != 0)) || (st = upload(b, in, c->stream))) {
         abea_batch_destroy(b);
         return st;
     }
@@ -789,6 +824,152 @@ extern "C" abea_status_t abea_batch_read_bands(abea_ctx_t* c, abea_batch_t* b, i
     return ABEA_OK;
 }
 
+// ---------------------------------------------------------------- adjoint
+// Queues the backward kernel over the stored paths of the last run.
+static abea_status_t queue_backward(abea_ctx* c, abea_batch* b, bool model_grad) {
+    if (model_grad)
+        CUDA_TRY(cudaMemsetAsync(b->d_grad_model, 0, sizeof(double) * 2 * ABEA_NUM_KMER, c->stream));
+    AdjArgs a{b->d_reads, b->n_reads, b->var_aware, b->d_seq, b->d_model, b->d_ev_mean, b->d_pairs,
+              b->d_path_len, b->d_path_flags, b->d_grad_sc, b->d_gn, b->d_path_em,
+              model_grad ? b->d_grad_model : nullptr, b->d_adj_status};
+    cudaError_t e = launch_adjoint(a, c->stream);
+    if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_backward(abea_ctx_t* c, abea_batch_t* b, double* grad_scalings,
+                                             double* grad_model, double* path_emission, int32_t* read_status) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_backward: null argument");
+    if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
+    if (!b->ran) return fail(ABEA_ERR_INVALID_ARG, "batch has not been run");
+    CUDA_TRY(cudaSetDevice(c->device));
+    if (b->n_reads == 0) {
+        if (grad_model) memset(grad_model, 0, sizeof(double) * 2 * ABEA_NUM_KMER);
+        return ABEA_OK;
+    }
+    abea_status_t st = queue_backward(c, b, grad_model != nullptr);
+    if (st) return st;
+    const size_t n = (size_t)b->n_reads;
+    if (grad_scalings)
+        CUDA_TRY(cudaMemcpyAsync(grad_scalings, b->d_grad_sc, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    if (grad_model)
+        CUDA_TRY(cudaMemcpyAsync(grad_model, b->d_grad_model, sizeof(double) * 2 * ABEA_NUM_KMER,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    if (path_emission)
+        CUDA_TRY(cudaMemcpyAsync(path_emission, b->d_path_em, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    if (read_status)
+        CUDA_TRY(cudaMemcpyAsync(read_status, b->d_adj_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                 c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return ABEA_OK;
+}
+
+// Host copy of the per-read scalings -> descriptors (and their shortcut flag).
+static void apply_scalings(abea_batch* b, const abea_scalings_t* sc) {
+    for (int32_t i = 0; i < b->n_reads; ++i) {
+        ReadDesc& r = b->reads[(size_t)i];
+        r.scale = sc[i].scale;
+        r.shift = sc[i].shift;
+        r.var = sc[i].var;
+        r.log_var = sc[i].log_var;
+        if (!r.skip) r.nonpos = model_nonpos(b->min_lsd, r.log_var, b->var_aware);
+    }
+}
+
+static abea_status_t upload_reads(abea_ctx* c, abea_batch* b) {
+    if (b->n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaMemcpyAsync(b->d_reads, b->reads.data(), sizeof(ReadDesc) * b->reads.size(),
+                             cudaMemcpyHostToDevice, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));  // the host descriptors may change next
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_batch_set_scalings(abea_ctx_t* c, abea_batch_t* b, const abea_scalings_t* sc) {
+    if (!c || !b || (!sc && b->n_reads > 0)) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_set_scalings: null argument");
+    if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
+    CUDA_TRY(cudaSetDevice(c->device));
+    apply_scalings(b, sc);
+    return upload_reads(c, b);
+}
+
+// Gauss-Newton on (shift, scale): the residuals (x - scale*mu - shift)/sd of the
+// emitting cells of the fixed path are linear in (shift, scale), so one step
+// solves the weighted least-squares problem on that path exactly; re-aligning
+// with the new scalings moves the path, hence the iterations.  Far from the
+// truth the first paths are partly misaligned and bias the fit, so iteration
+// `it` of `n` aligns with every emission stdv multiplied by
+// T = first_temperature^((n-1-it)/(n-1)) (the last one with T = 1).  A common
+// factor on every sd of a read leaves its GN solution unchanged, so the normal
+// equations are taken from the tempered run as they are.
+extern "C" abea_status_t abea_batch_recalibrate(abea_ctx_t* c, abea_batch_t* b, int32_t iterations,
+                                                double first_temperature, abea_scalings_t* out) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_recalibrate: null argument");
+    if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
+    if (iterations < 0) return fail(ABEA_ERR_INVALID_ARG, "iterations < 0");
+    if (!(first_temperature > 0.0) || !std::isfinite(first_temperature))
+        return fail(ABEA_ERR_INVALID_ARG, "first_temperature must be positive");
+    CUDA_TRY(cudaSetDevice(c->device));
+    const size_t n = (size_t)b->n_reads;
+    std::vector<abea_scalings_t> sc(n), run_sc(n);
+    for (size_t i = 0; i < n; ++i) {
+        const ReadDesc& r = b->reads[i];
+        sc[i] = abea_scalings_t{r.scale, r.shift, r.var, r.log_var};
+    }
+    std::vector<double> gn(5 * n);
+    std::vector<int32_t> ast(n);
+    const int32_t va0 = b->var_aware;
+    abea_status_t st = ABEA_OK;
+    for (int32_t it = 0; it < iterations && n > 0 && !st; ++it) {
+        const double T = iterations > 1 && first_temperature != 1.0
+                             ? pow(first_temperature, (double)(iterations - 1 - it) / (double)(iterations - 1))
+                             : 1.0;
+        b->var_aware = (va0 || T != 1.0) ? 1 : 0;
+        for (size_t i = 0; i < n; ++i) {
+            run_sc[i] = sc[i];
+            if (T != 1.0) {
+                run_sc[i].var = va0 ? (float)((double)sc[i].var * T) : (float)T;
+                run_sc[i].log_var = va0 ? (float)((double)sc[i].log_var + log(T)) : (float)log(T);
+            }
+        }
+        apply_scalings(b, run_sc.data());
+        if ((st = upload_reads(c, b)) || (st = run_batch(c, b)) || (st = queue_backward(c, b, false))) break;
+        cudaError_t e = cudaMemcpyAsync(gn.data(), b->d_gn, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(ast.data(), b->d_adj_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            st = fail(ABEA_ERR_CUDA, "recalibration: %s", cudaGetErrorString(e));
+            break;
+        }
+        for (size_t i = 0; i < n; ++i) {
+            if (ast[i] != 0 || b->reads[i].skip) continue;
+            const double* h = &gn[5 * i];
+            const double det = h[0] * h[2] - h[1] * h[1];
+            if (!(det > 1e-12 * h[0] * h[2])) continue;  // fewer than two distinct levels on the path
+            // [h0 h1; h1 h2] (d_shift, d_scale) = -(t1, t2)
+            const double ds = (-h[3] * h[2] + h[4] * h[1]) / det;
+            const double dk = (-h[4] * h[0] + h[3] * h[1]) / det;
+            const double ns = (double)sc[i].shift + ds, nk = (double)sc[i].scale + dk;
+            if (!std::isfinite(ns) || !std::isfinite(nk) || !(nk > 0.0)) continue;
+            sc[i].shift = (float)ns;
+            sc[i].scale = (float)nk;
+        }
+    }
+    // the batch keeps its own emission mode and the final scalings
+    b->var_aware = va0;
+    apply_scalings(b, sc.data());
+    if (st) return st;
+    if (n > 0 && iterations > 0) {
+        if ((st = upload_reads(c, b)) || (st = run_batch(c, b))) return st;
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    if (out)
+        for (size_t i = 0; i < n; ++i) out[i] = sc[i];
+    return ABEA_OK;
+}
+
 // ---------------------------------------------------------------- one-call batch
 static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_aligned_pair_t* pairs,
                                       int32_t* n_pairs) {
@@ -801,7 +982,7 @@ static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_al
         c->scratch->ctx = c;
     }
     abea_batch* b = c->scratch;
-    if ((st = plan(b, in)) || (st = ensure_device(b, c->store_scores != 0))) return st;
+    if ((st = plan(b, in, (int)c->var_aware)) || (st = ensure_device(b, c->store_scores != 0))) return st;
     CUDA_TRY(cudaEventRecord(c->ev[4], c->stream));
     if ((st = upload(b, in, c->stream))) return st;
     CUDA_TRY(cudaEventRecord(c->ev[5], c->stream));

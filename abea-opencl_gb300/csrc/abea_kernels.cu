@@ -615,7 +615,7 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
     const uint8_t* trace = a.trace + r.band_off * kSlots;
     const int32_t* bk0 = a.band_k0 + r.band_off;
     const int cap = r.out_cap;
-    int n_out = 0, max_gap = 0, status = 0, last_k = n_kmers - 1;
+    int n_out = 0, max_gap = 0, status = 0, last_k = n_kmers - 1, last_from = 0;
 
     if (best > -INFINITY) {
         // A finite end: the path only visits computed cells.  Walked by lane 0
@@ -650,6 +650,7 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
                     ++n_out;
                     last_k = cur_k;
                     const uint32_t from = tb[((lb >> 2) << 9) | (slot << 2) | (lb & 3)];
+                    last_from = (int)from;
                     // D: band-2, slot-1; U: band-1, same slot; L: band-1, slot-1
                     const bool is_u = from == ABEA_FROM_U, is_l = from == ABEA_FROM_L;
                     lb -= (is_u || is_l) ? 1 : 2;
@@ -684,17 +685,21 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
                 break;
             }
             const int64_t b2 = flat / kBand;
-            step_back(trace[trace_index(b2, (bk0[b2] + (int)(flat - b2 * kBand)) & 127)], cur_k, cur_e, gap, max_gap);
+            const uint32_t from = trace[trace_index(b2, (bk0[b2] + (int)(flat - b2 * kBand)) & 127)];
+            last_from = (int)from;
+            step_back(from, cur_k, cur_e, gap, max_gap);
         }
     }
     n_out = __shfl_sync(kFull, n_out, 0);
     max_gap = __shfl_sync(kFull, max_gap, 0);
     status = __shfl_sync(kFull, status, 0);
     last_k = __shfl_sync(kFull, last_k, 0);
+    last_from = __shfl_sync(kFull, last_from, 0);
     __syncwarp();
     __threadfence_block();
 
     int result = 0;
+    bool reversed = false;
     if (status == 0 && n_out > 0) {
         // QC (GPU/align_cuda.cl:856-882).  After the reversal out[0] is the last
         // cell walked and out[n-1] the first, so spanned <=> last_k == 0.
@@ -752,6 +757,7 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
                 out[n_out - 1 - i2] = x;
             }
             result = n_out;
+            reversed = true;
         }
     } else if (status != 0) {
         result = status;
@@ -760,6 +766,15 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
         a.n_pairs[ri] = result;
         a.best_scores[ri] = best;
         a.status[ri] = status;
+        if (a.path_len) {
+            // the path for the adjoint: its length, whether the output holds it in
+            // walk order or reversed, and the move into its last walked cell
+            a.path_len[ri] = n_out;
+            a.path_flags[ri] = (reversed ? kPathReversed : 0) | (n_out > cap ? kPathTruncated : 0) |
+                               (best > -INFINITY ? 0 : kPathNoEnd) | (status != 0 ? kPathError : 0) |
+                               (last_from << 8);
+            a.best_event[ri] = best_e;
+        }
     }
 }
 
@@ -1004,3 +1019,88 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     }
     return ABEA_OK;
 }
+
+// ---------------------------------------------------------------- adjoint
+// Gradient of the best path's log-likelihood along the fixed path of a finished
+// forward run: the transitions and trims do not depend on the scalings or the
+// pore model, so d(score)/d(theta) is the sum, over the path cells entered by a
+// D or U move (the cells whose emission the score contains), of
+//   d em/d shift = a/sd, d em/d scale = a*mu/sd, d em/d mu_k = a*scale/sd,
+//   d em/d stdv_k = (a^2 - 1)/stdv_k, d em/d var = (a^2 - 1)/var (var-aware only),
+// with em = log_inv_sqrt_2pi - log(sd) - a^2/2, a = (x - (scale*mu + shift))/sd,
+// sd = stdv (times var when var-aware).  Everything is evaluated and accumulated
+// in FP64.  Also accumulated: the Gauss-Newton normal equations of the residuals
+// a in (shift, scale) — J^T J and J^T a with J = (-1/sd, -mu/sd) — and the FP64
+// emission sum of the path.
+namespace abea {
+
+__global__ void __launch_bounds__(32) abea_adjoint_kernel(AdjArgs a) {
+    const int ri = blockIdx.x, lane = threadIdx.x;
+    if (ri >= a.n_reads) return;
+    const ReadDesc r = a.reads[ri];
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // shift, scale, var, j11, j12, j22, t1, t2, em
+    int st = 0;
+    const int len = r.skip ? 0 : a.path_len[ri];
+    const int flags = r.skip ? 0 : a.path_flags[ri];
+    if (len > 0 && (flags & (kPathTruncated | kPathNoEnd | kPathError))) {
+        st = (flags & kPathTruncated) ? ABEA_ERR_CAPACITY : ABEA_ERR_UNDEFINED;
+    } else if (len > 0) {
+        const abea_aligned_pair_t* out = a.pairs + r.out_off;
+        const bool rev = (flags & kPathReversed) != 0;
+        const int last_from = flags >> 8;
+        const char* s = a.seq + r.seq_off;
+        const double scale = r.scale, shift = r.shift, var = r.var, log_var = r.log_var;
+        for (int j = lane; j < len; j += 32) {
+            const int w = rev ? len - 1 - j : j;  // walk position, 0 = best end
+            const abea_aligned_pair_t c = out[j];
+            bool counted;
+            if (w < len - 1) {
+                const abea_aligned_pair_t nx = rev ? out[j - 1] : out[j + 1];
+                counted = nx.read_pos == c.read_pos - 1;  // D or U: the next walked cell is one event back
+            } else {
+                counted = last_from != (int)ABEA_FROM_L;
+            }
+            if (!counted) continue;
+            uint32_t rank = 0;
+#pragma unroll
+            for (int q = 0; q < ABEA_KMER_SIZE; ++q) rank = (rank << 2) | base_rank(s[c.ref_pos + q]);
+            const abea_model_t m = a.model[rank];
+            const double mu = m.level_mean, sig = m.level_stdv;
+            const double sd = a.var_aware ? sig * var : sig;
+            const double lsd = a.var_aware ? (double)m.level_log_stdv + log_var : (double)m.level_log_stdv;
+            const double x = a.ev_mean[r.ev_off + c.read_pos];
+            const double isd = 1.0 / sd;
+            const double av = (x - (scale * mu + shift)) * isd;
+            acc[0] += av * isd;
+            acc[1] += av * mu * isd;
+            if (a.var_aware) acc[2] += (av * av - 1.0) / var;
+            acc[3] += isd * isd;
+            acc[4] += mu * isd * isd;
+            acc[5] += mu * mu * isd * isd;
+            acc[6] -= av * isd;
+            acc[7] -= av * mu * isd;
+            acc[8] += -0.91893853320467274 - lsd - 0.5 * av * av;
+            if (a.grad_model) {
+                atomicAdd(&a.grad_model[2 * rank], av * scale * isd);
+                atomicAdd(&a.grad_model[2 * rank + 1], (av * av - 1.0) / sig);
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_xor_sync(kFull, acc[i], off);
+    if (lane == 0) {
+        for (int i = 0; i < 3; ++i) a.grad_scalings[3 * ri + i] = acc[i];
+        for (int i = 0; i < 5; ++i) a.gn[5 * ri + i] = acc[3 + i];
+        a.path_em[ri] = acc[8];
+        a.adj_status[ri] = st;
+    }
+}
+
+cudaError_t launch_adjoint(const AdjArgs& a, cudaStream_t stream) {
+    if (a.n_reads > 0) abea_adjoint_kernel<<<a.n_reads, 32, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace abea

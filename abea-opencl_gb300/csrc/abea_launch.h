@@ -60,7 +60,32 @@ struct PostArgs {
     int32_t* n_pairs;
     float* best_scores;
     int32_t* status;  // per-read abea_status_t (0 = ok)
+    int32_t* path_len;    // optional (nullptr): path length, for the adjoint
+    int32_t* path_flags;  // kPath* bits | move into the last walked cell << 8
+    int32_t* best_event;  // event of the best end
 };
+
+constexpr int32_t kPathReversed = 1, kPathTruncated = 2, kPathNoEnd = 4, kPathError = 8;
+
+struct AdjArgs {
+    const ReadDesc* reads;
+    int n_reads;
+    int var_aware;
+    const char* seq;
+    const abea_model_t* model;
+    const float* ev_mean;
+    const abea_aligned_pair_t* pairs;
+    const int32_t* path_len;
+    const int32_t* path_flags;
+    double* grad_scalings;  // [n][3]: d/d shift, scale, var
+    double* gn;             // [n][5]: J^T J (11, 12, 22), J^T r (1, 2) of the (shift, scale) residuals
+    double* path_em;        // [n]: sum of the path's emissions (FP64)
+    double* grad_model;     // [4096][2]: d/d level_mean, level_stdv, summed over reads
+    int32_t* adj_status;    // [n]: 0, or why the read has no gradient
+};
+
+// Backward pass over the stored paths of a finished forward run.
+cudaError_t launch_adjoint(const AdjArgs& a, cudaStream_t stream);
 
 struct LaunchArgs {
     PreArgs pre;

@@ -101,7 +101,9 @@ typedef enum {
     ABEA_OPT_STORE_SCORES = 1,  /* 1: keep every band's scores in HBM (reference layout, GPU/align_cuda.c:573-577) */
     ABEA_OPT_USE_GRAPH = 2,     /* BATCHED only: 1 = replay the three stages as one CUDA graph */
     ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide (4-warp) shape; 0 = autotuned */
-    ABEA_OPT_SPIN_LIMIT = 4     /* upper bound on any device-side wait, in polling iterations */
+    ABEA_OPT_SPIN_LIMIT = 4,    /* upper bound on any device-side wait, in polling iterations */
+    ABEA_OPT_VAR_AWARE = 5      /* 1: emissions use level_stdv*var and level_log_stdv+log_var (the
+                                   reference ignores var, GPU/align_cuda.cl:509); taken at batch creation */
 } abea_option_t;
 
 typedef struct abea_ctx abea_ctx_t;
@@ -232,6 +234,40 @@ abea_status_t abea_ctx_flush_l2(abea_ctx_t *ctx);
  * out[5]: division wrong, division declined, sum wrong, sum declined, cases.
  * "wrong" must be 0; "declined" cases take the FP64 path in the kernels. */
 abea_status_t abea_selftest_arith(int64_t cases, uint64_t seed, int64_t *out);
+
+/* ---- adjoint (no counterpart in the reference) ---------------------------
+ * Gradients of each read's best-path log-likelihood, evaluated in FP64 along the
+ * path that the last run of the batch stored (the moves and trims on a fixed path
+ * do not depend on the parameters; only the emissions of the cells entered by a
+ * step or a stay do).  The batch must have been run (abea_batch_run +
+ * abea_batch_sync) or aligned.  Outputs (host arrays, each may be NULL):
+ *   grad_scalings[n_reads*3]: d/d shift, d/d scale, d/d var (var only counts
+ *       with ABEA_OPT_VAR_AWARE; 0 otherwise);
+ *   grad_model[4096*2]: d/d level_mean, d/d level_stdv of every k-mer (rank
+ *       order, summed over the reads that have a gradient);
+ *   path_emission[n_reads]: the FP64 sum of the emissions on the path;
+ *   read_status[n_reads]: 0, or the abea_status_t saying why the read has no
+ *       gradient (no path, truncated path); those reads' entries are 0.
+ * Reads whose alignment failed the quality checks still have a path and a
+ * gradient. */
+abea_status_t abea_batch_backward(abea_ctx_t *ctx, abea_batch_t *batch, double *grad_scalings,
+                                  double *grad_model, double *path_emission, int32_t *read_status);
+
+/* Replaces the per-read scalings of a device-resident batch (host array
+ * [n_reads]); the next abea_batch_run aligns with them. */
+abea_status_t abea_batch_set_scalings(abea_ctx_t *ctx, abea_batch_t *batch, const abea_scalings_t *scalings);
+
+/* Gauss-Newton recalibration of (shift, scale) per read: `iterations` rounds of
+ * align -> fixed-path normal equations (residuals (x - scale*mu - shift)/stdv of the
+ * emitting cells) -> step.  Round it of n aligns with every emission stdv
+ * multiplied by first_temperature^((n-1-it)/(n-1)) (annealing: the last round,
+ * and every round when first_temperature = 1, uses the model as it is); 5 suits
+ * scalings that are off by several pA and several percent.  A read whose path is
+ * missing or whose normal equations are singular keeps its scalings.  The batch
+ * is left aligned with the final scalings, which are written to out[n_reads]
+ * (may be NULL). */
+abea_status_t abea_batch_recalibrate(abea_ctx_t *ctx, abea_batch_t *batch, int32_t iterations,
+                                     double first_temperature, abea_scalings_t *out);
 
 /* ---- no-allocation entry point ------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -106,6 +106,7 @@ int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
                      abea_scalings_t sc, uint32_t flags, oracle_debug_t *dbg) {
     if (dbg) {
         dbg->best_score = -INFINITY;
+        dbg->last_from = FROM_L;
         dbg->best_event = 0;
         dbg->sum_emission = 0.0;
         dbg->path_len = 0;
@@ -228,7 +229,7 @@ int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
      * (into the next read's slot in a batch); the walk continues without
      * writing so that the QC verdict is still the reference's, and such a read
      * is reported as ABEA_ERR_CAPACITY only when it passes QC. */
-    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0, last_k = cur_k;
+    int32_t n_out = 0, gap = 0, max_gap = 0, status = 0, last_k = cur_k, last_from = FROM_L;
     double sum_em = 0.0;
     float sum_em_f = 0.0f;
     double n_aligned = 0.0;
@@ -253,6 +254,7 @@ int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
             break;
         }
         uint8_t from = trace[idx];
+        last_from = from;
         if (from == FROM_D) {
             cur_k -= 1;
             cur_e -= 1;
@@ -275,6 +277,7 @@ int32_t oracle_align(abea_aligned_pair_t *out, int32_t out_cap, const char *seq,
         dbg->sum_emission = (flags & ORACLE_QC_FLOAT) ? (double)sum_em_f : sum_em;
         dbg->path_len = n_out;
         dbg->max_gap = max_gap;
+        dbg->last_from = last_from;
     }
     free(ranks);
     free(bands);
@@ -506,4 +509,59 @@ void oracle_align_batch(int32_t n_reads, const char *read, const int64_t *read_p
     free(th);
     free(order);
     free(key);
+}
+
+/* ---- FP64 path adjoint (no counterpart in the reference) ----
+ * The best-path score is the sum of the transition and trim log-probabilities
+ * along the path (independent of the scalings and the pore model) and of the
+ * emissions of the cells entered by a step (D) or a stay (U).  walk[j+1] is the
+ * predecessor of walk[j], so walk[j] emits iff walk[j+1].read_pos ==
+ * walk[j].read_pos - 1; the last walked cell emits iff it was entered by D or U. */
+double oracle_path_adjoint(const abea_aligned_pair_t *walk, int32_t n, int32_t last_from,
+                           const char *seq, const abea_event_t *events, const abea_model_t *model,
+                           abea_scalings_t sc, const double *theta, int32_t d_kmer, double d_mean,
+                           double d_stdv, uint32_t flags, double *grad3, double *gn5,
+                           double *grad_model) {
+    const double shift = theta ? theta[0] : (double)sc.shift;
+    const double scale = theta ? theta[1] : (double)sc.scale;
+    const double var = theta ? theta[2] : (double)sc.var;
+    const int var_aware = (flags & ORACLE_VAR_AWARE) != 0;
+    double g[3] = {0, 0, 0}, h[5] = {0, 0, 0, 0, 0}, em_sum = 0.0;
+    for (int32_t j = 0; j < n; ++j) {
+        int emits = j + 1 < n ? walk[j + 1].read_pos == walk[j].read_pos - 1 : last_from != FROM_L;
+        if (!emits) continue;
+        uint32_t rank = oracle_kmer_rank(seq + walk[j].ref_pos);
+        const abea_model_t *m = &model[rank];
+        double mu = m->level_mean, sig = m->level_stdv, lsd = m->level_log_stdv;
+        if ((int32_t)rank == d_kmer) {
+            mu += d_mean;
+            lsd += log1p(d_stdv / sig);
+            sig += d_stdv;
+        }
+        double sd = sig;
+        if (var_aware) {
+            sd = sig * var;
+            lsd += (double)sc.log_var + log(var / (double)sc.var);
+        }
+        double x = events[walk[j].read_pos].mean;
+        double a = (x - (scale * mu + shift)) / sd;
+        em_sum += -0.91893853320467274178 - lsd - 0.5 * a * a;
+        g[0] += a / sd;
+        g[1] += a * mu / sd;
+        if (var_aware) g[2] += (a * a - 1.0) / var;
+        h[0] += 1.0 / (sd * sd);
+        h[1] += mu / (sd * sd);
+        h[2] += mu * mu / (sd * sd);
+        h[3] -= a / sd;
+        h[4] -= a * mu / sd;
+        if (grad_model) {
+            grad_model[2 * rank] += a * scale / sd;
+            grad_model[2 * rank + 1] += (a * a - 1.0) / sig;
+        }
+    }
+    if (grad3)
+        for (int i = 0; i < 3; ++i) grad3[i] = g[i];
+    if (gn5)
+        for (int i = 0; i < 5; ++i) gn5[i] = h[i];
+    return em_sum;
 }

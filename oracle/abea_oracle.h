@@ -38,6 +38,7 @@ typedef struct {
     double sum_emission;                   /* QC sum along the path */
     int32_t path_len;                      /* pairs on the path before QC */
     int32_t max_gap;
+    int32_t last_from;                     /* move into the last walked cell (0=D, 1=U, 2=L) */
 } oracle_debug_t;
 
 /* One read.  Returns the number of pairs written to out (0 = QC failure), or
@@ -71,6 +72,23 @@ int32_t oracle_align_f64(abea_aligned_pair_t *out, int32_t out_cap, const char *
  * (GPU/align_cuda.cl:85-110, align_swi.cl:77-111). */
 float oracle_emission(float event_mean, const abea_model_t *m, abea_scalings_t scaling,
                       uint32_t flags);
+
+/* FP64 adjoint of one read's fixed path (no counterpart in the reference).
+ * walk[0..n) in walk order (walk[0] = best end), last_from = the move into
+ * walk[n-1].  Emissions in double: a = (x - (scale*mu + shift))/sd,
+ * em = -log(sqrt(2 pi)) - log_stdv - a^2/2, sd = stdv (times var and log_stdv
+ * plus log var with ORACLE_VAR_AWARE).  theta = (shift, scale, var) in double
+ * (NULL: the scalings'); k-mer d_kmer (-1: none) has level_mean + d_mean and
+ * level_stdv + d_stdv (log stdv moved by log1p(d_stdv/stdv)).  Returns the sum
+ * of the emitting cells' emissions; grad3 = d/d(shift, scale, var), gn5 = Gauss-
+ * Newton sums (J^T J 11, 12, 22; J^T r 1, 2) of the residuals a in (shift,
+ * scale), grad_model[4096*2] += d/d(level_mean, level_stdv).  Any output may be
+ * NULL. */
+double oracle_path_adjoint(const abea_aligned_pair_t *walk, int32_t n, int32_t last_from,
+                           const char *seq, const abea_event_t *events, const abea_model_t *model,
+                           abea_scalings_t sc, const double *theta, int32_t d_kmer, double d_mean,
+                           double d_stdv, uint32_t flags, double *grad3, double *gn5,
+                           double *grad_model);
 
 /* Rank of the 6-mer starting at s (GPU/align_cuda.cl:22-51). */
 uint32_t oracle_kmer_rank(const char *s);

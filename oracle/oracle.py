@@ -35,7 +35,7 @@ class _Debug(C.Structure):
     _fields_ = [
         ("bands", C.c_void_p), ("trace", C.c_void_p), ("band_lower_left", C.c_void_p),
         ("best_score", C.c_float), ("best_event", C.c_int32), ("sum_emission", C.c_double),
-        ("path_len", C.c_int32), ("max_gap", C.c_int32),
+        ("path_len", C.c_int32), ("max_gap", C.c_int32), ("last_from", C.c_int32),
     ]
 
 
@@ -67,6 +67,10 @@ def lib():
         L.oracle_emission.argtypes = [C.c_float, C.c_void_p, _Scalings, C.c_uint32]
         L.oracle_add3.restype = C.c_float
         L.oracle_add3.argtypes = [C.c_float, C.c_double, C.c_float]
+        L.oracle_path_adjoint.restype = C.c_double
+        L.oracle_path_adjoint.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_char_p, C.c_void_p,
+                                          C.c_void_p, _Scalings, C.c_void_p, C.c_int32, C.c_double,
+                                          C.c_double, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
         L.oracle_n_bands.restype = C.c_int64
         L.oracle_n_bands.argtypes = [C.c_int32, C.c_int32]
         _lib = L
@@ -102,9 +106,14 @@ def align(seq: bytes, events: np.ndarray, model: np.ndarray, scalings, flags: in
         dbg.bands, dbg.trace, dbg.band_lower_left = _ptr(bands), _ptr(trace), _ptr(bll)
     n = L.oracle_align(_ptr(out), cap, bytes(seq), len(seq), _ptr(events), n_ev, _ptr(model),
                        _sc(scalings), flags, C.byref(dbg))
+    # the path in walk order (best end first): reversed on success, as walked otherwise
+    if n > 0:
+        walk = out[:n][::-1].copy()
+    else:
+        walk = out[: min(dbg.path_len, cap)].copy()
     info = dict(best_score=dbg.best_score, best_event=dbg.best_event,
                 sum_emission=dbg.sum_emission, path_len=dbg.path_len, max_gap=dbg.max_gap,
-                bands=bands, trace=trace, bll=bll)
+                last_from=dbg.last_from, walk=walk, bands=bands, trace=trace, bll=bll)
     return out[: max(n, 0)], n, info
 
 
@@ -140,6 +149,24 @@ def align_batch(batch, flags: int = 0, threads: int | None = None):
 def emission(x: float, model_entry, scalings, flags: int = 0) -> float:
     m = np.ascontiguousarray(np.asarray([model_entry], dtype=MODEL_DTYPE))
     return float(lib().oracle_emission(x, _ptr(m), _sc(scalings), flags))
+
+
+def path_adjoint(walk, last_from: int, seq: bytes, events, model, scalings, flags: int = 0,
+                 theta=None, kmer: int = -1, d_mean: float = 0.0, d_stdv: float = 0.0,
+                 want_model: bool = False):
+    """FP64 adjoint of one fixed path (walk order, best end first).  Returns
+    (emission_sum, grad[shift, scale, var], gn[5], grad_model[4096,2] or None)."""
+    walk = np.ascontiguousarray(walk, dtype=PAIR_DTYPE)
+    events = np.ascontiguousarray(events, dtype=EVENT_DTYPE)
+    model = np.ascontiguousarray(model, dtype=MODEL_DTYPE)
+    g = np.zeros(3)
+    gn = np.zeros(5)
+    gm = np.zeros((4096, 2)) if want_model else None
+    th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+    em = lib().oracle_path_adjoint(_ptr(walk), len(walk), int(last_from), bytes(seq), _ptr(events),
+                                   _ptr(model), _sc(scalings), _ptr(th), int(kmer), float(d_mean),
+                                   float(d_stdv), flags, _ptr(g), _ptr(gn), _ptr(gm))
+    return em, g, gn, gm
 
 
 def add3(a: float, b: float, c: float) -> float:
