@@ -104,6 +104,32 @@ __device__ __forceinline__ float exact_sum(float a, float bh, float bl, float c,
     return hp;
 }
 
+// The skip candidate RN32(RN64(a + B)) for float a and double B = bh + bl + r:
+// Fast2Sum gives s + e = a + bh exactly when |a| >= |bh|, the exact sum lies
+// within 2^-47 (|a| + |bh|) of s + (e + bl) (RN64's own rounding included), and
+// equal roundings of the bracket +-eb, eb = 2^-42 (|a| + |bh|), prove the result
+// as in exact_sum.  a = -inf gives -inf (proven); otherwise ok = false when not
+// proven, which happens only while |a| < |bh| (a read's first bands).
+__device__ __forceinline__ float exact_skip(float a, float bh, float bl, bool& ok) {
+    const float s = __fadd_rn(a, bh);
+    const float e = __fsub_rn(bh, __fsub_rn(s, a));
+    const float t = __fadd_rn(e, bl);
+    const float eb = __fmul_rn(__fadd_rn(fabsf(a), fabsf(bh)), kErrScale);
+    const float hp = __fadd_rn(s, __fadd_rn(t, eb));
+    const float hm = __fadd_rn(s, __fsub_rn(t, eb));
+    const bool a_inf = a == -INFINITY;
+    ok = ((hp == hm) && (fabsf(a) >= fabsf(bh))) || a_inf;
+    return a_inf ? -INFINITY : hp;
+}
+
+// max(best_du, l) with L winning ties (GPU/align_cuda.cl:536-542); all three
+// candidates -inf resolve to -inf, FROM_L.
+__device__ __forceinline__ float pick_l(float best_du, uint32_t from_du, float l, uint32_t& from) {
+    const float best = l > best_du ? l : best_du;
+    from = (best == l) ? ABEA_FROM_L : from_du;
+    return best;
+}
+
 // exact_sum that also accepts a = -inf (result -inf, exact for finite c).
 __device__ __forceinline__ float exact_sum_inf(float a, float bh, float bl, float c, bool& ok) {
     bool ok1;
@@ -210,7 +236,7 @@ __device__ __forceinline__ float cell_l(float d, float u, float left, const Cell
 
 // The reference's arithmetic verbatim (IEEE division, FP64 adds): the fallback
 // when an exactness proof does not go through.
-static __device__ __noinline__ float cell_slow(float diag, float up, float left, float x, float gm, float sd, float k1,
+static __device__ __forceinline__ float cell_slow(float diag, float up, float left, float x, float gm, float sd, float k1,
                                         const CellConsts c, uint32_t& from) {
     float em = emission_ieee(x, gm, sd, k1);
     float d = __double2float_rn(__dadd_rn(__dadd_rn((double)diag, c.lp_step), (double)em));

@@ -12,9 +12,11 @@
 //   warp — one warp per read, lane l holds k-mer slots 4l..4l+3.  Neighbour
 //          scores move by one shuffle per band, the band move is decided from two
 //          shuffled end cells; no block barrier.  Most work per SM.
-//   wide — four warps per read, one slot per thread, edge cells exchanged in
-//          shared memory with one barrier per band.  Shortest band latency: used
-//          for the longest reads of a batch.
+//   wide — sixteen warps per read in four groups of 128 threads (one slot per
+//          thread each): one group runs only the band-to-band chain, the others
+//          prepare emissions, diagonal candidates and bookkeeping ahead of it;
+//          cells exchanged in shared memory with one barrier per band.  Shortest
+//          band latency: used for the longest reads of a batch.
 // Forms:
 //   plain   — pre, core (warp shape, one block per read), post (one block per
 //             read): the reference's three launches.
@@ -23,6 +25,7 @@
 //             reads longest-first from a device queue; every read's post runs in
 //             the warp that filled it, right after its fill (trace still in L2).
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include <stdio.h>
@@ -120,7 +123,8 @@ __global__ void __launch_bounds__(128) abea_pre_kernel(PreArgs a) {
 // event means in a 256-entry ring indexed by event & 255.  Chunks of 16 are
 // copied with cp.async as soon as the entries they overwrite have left the band:
 // a k-mer chunk [c, c+16) once c+15 <= k0+127, an event chunk once c+15 <= e0+156.
-struct Rings {
+// 16-byte aligned: cp.async copies 16 bytes and the warp shape reads float4s.
+struct alignas(16) Rings {
     float gm[kSlots];
     float sd[kSlots];
     float rsd[kSlots];
@@ -263,68 +267,16 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
     const int sl_last = (n_kmers - 1) & 127;
     uint32_t tw0 = 0u, tw1 = lane == 31 ? (ABEA_FROM_U << 24) : 0u, tw2 = 0u, tw3 = 0u;
 
-    for (int b = 2; b < n_bands; ++b) {
-        if ((b & 3) == 0) {
-            if (rings_step(rg, rs, a, r, lane, k0, e0, 6)) __syncwarp();
-        }
-        // ---- exchange: end cells for the placement, left neighbour of slot 4*lane
-        const int sl = k0 & 127, su = (k0 + kBand - 1) & 127;
-        const float ll = __shfl_sync(kFull, sel4(S1, sl & 3), sl >> 2);
-        const float ur = __shfl_sync(kFull, sel4(S1, su & 3), su >> 2);
-        const float left0 = __shfl_sync(kFull, S1[3], (lane + 31) & 31);
-        const float left[4] = {left0, S1[0], S1[1], S1[2]};
-        // ---- up candidates of band b
-        float u[4];
-        bool oku[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) u[j] = cell_u(S1[j], nc[j], cc, oku[j]);
-        // ---- band b+1's emission side (placement-independent)
-        const float4 gm4 = *reinterpret_cast<const float4*>(&rg.gm[4 * lane]);
-        const float4 sd4 = *reinterpret_cast<const float4*>(&rg.sd[4 * lane]);
-        const float4 rs4 = *reinterpret_cast<const float4*>(&rg.rsd[4 * lane]);
-        const float4 k14 = *reinterpret_cast<const float4*>(&rg.k1[4 * lane]);
-        const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w}, sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
-        const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w}, k1v[4] = {k14.x, k14.y, k14.z, k14.w};
-        NextCell nn[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            nn[j] = next_cell(left[j], rg.ev[(ep[j] + 2) & (kEvRing - 1)], gmv[j], sdv[j], rsv[j], k1v[j], cc);
-        // ---- band placement (Suzuki-Kasahara), GPU/align_cuda.cl:394-430
-        const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
-        k0 += right ? 1 : 0;
-        e0 += right ? 0 : 1;
-        int lo, hi;
-        band_range(k0, e0, n_events, n_kmers, lo, hi);
-        // ---- skip candidate, comparison; rare tiers in one branch
-        float best[4];
-        uint32_t from[4];
-        bool valid[4], need_l[4], bad[4];
-        bool rare = false;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int o = (4 * lane + j - k0) & 127;
-            ep[j] = e0 - o;
-            valid[j] = (o >= lo) && (o < hi);
-            best[j] = cell_b(nc[j].d, u[j], left[j], cc, from[j], need_l[j]);
-            need_l[j] = need_l[j] && valid[j];
-            bad[j] = valid[j] && !(nc[j].ok && oku[j]);
-            rare |= need_l[j] || bad[j];
-        }
-        if (__any_sync(kFull, rare)) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (need_l[j]) {
-                    bool ok;
-                    best[j] = cell_l(nc[j].d, u[j], left[j], cc, from[j], ok);
-                    bad[j] |= !ok;
-                }
-                if (bad[j]) {
-                    const float x = rg.ev[ep[j] & (kEvRing - 1)];
-                    best[j] = cell_slow(LP[j], S1[j], left[j], x, gmv[j], sdv[j], k1v[j], cc, from[j]);
-                    ++slow;
-                }
-            }
-        }
+    // Band state kept across the exit to the slow path: a band in which a proof
+    // failed in any lane leaves the inner loop (warp-uniform) and is finished
+    // below with the reference's FP64 arithmetic, so that the inner loop holds
+    // no division routine and no FP64 code.
+    int b = 2, lo = 0, hi = 0;
+    float best[4], left[4];
+    uint32_t from[4];
+    bool valid[4], bad[4];
+    NextCell nn[4];
+    auto finish = [&]() {
         uint32_t word = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -335,11 +287,13 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         // and the last k-mer column read by the post stage (GPU/align_cuda.cl:722-746)
         const int ol = n_kmers - 1 - k0;
         if (k0 <= -1 || ol < kBand) {
-            if (k0 <= -1 && k0 >= -kBand && lane == 31) {
+            if (k0 <= -1) {  // uniform
                 const int e_t = e0 + 1 + k0;
                 const bool in = e_t >= 0 && e_t < n_events;
-                best[3] = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
-                word = (word & 0x00ffffffu) | (in ? (ABEA_FROM_U << 24) : 0u);
+                const float tv = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
+                const bool here = lane == 31 && k0 >= -kBand;
+                best[3] = here ? tv : best[3];
+                word = here ? ((word & 0x00ffffffu) | (in ? (ABEA_FROM_U << 24) : 0u)) : word;
             }
             if (ol >= lo && ol < hi && lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
         }
@@ -364,6 +318,75 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         if ((b & 31) == 31 || b == n_bands - 1) {
             if (lane <= (b & 31)) bk0[(b & ~31) + lane] = my_k0;
         }
+    };
+    while (true) {
+        bool to_slow = false;
+        for (; b < n_bands; ++b) {
+            if ((b & 3) == 0) {
+                if (rings_step(rg, rs, a, r, lane, k0, e0, 6)) __syncwarp();
+            }
+            // ---- exchange: end cells for the placement, left neighbour of slot 4*lane
+            const int sl = k0 & 127, su = (k0 + kBand - 1) & 127;
+            const float ll = __shfl_sync(kFull, sel4(S1, sl & 3), sl >> 2);
+            const float ur = __shfl_sync(kFull, sel4(S1, su & 3), su >> 2);
+            const float left0 = __shfl_sync(kFull, S1[3], (lane + 31) & 31);
+            left[0] = left0;
+            left[1] = S1[0];
+            left[2] = S1[1];
+            left[3] = S1[2];
+            // ---- up candidates of band b
+            float u[4];
+            bool oku[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) u[j] = cell_u(S1[j], nc[j], cc, oku[j]);
+            // ---- band b+1's emission side (placement-independent)
+            const float4 gm4 = *reinterpret_cast<const float4*>(&rg.gm[4 * lane]);
+            const float4 sd4 = *reinterpret_cast<const float4*>(&rg.sd[4 * lane]);
+            const float4 rs4 = *reinterpret_cast<const float4*>(&rg.rsd[4 * lane]);
+            const float4 k14 = *reinterpret_cast<const float4*>(&rg.k1[4 * lane]);
+            const float gmv[4] = {gm4.x, gm4.y, gm4.z, gm4.w}, sdv[4] = {sd4.x, sd4.y, sd4.z, sd4.w};
+            const float rsv[4] = {rs4.x, rs4.y, rs4.z, rs4.w}, k1v[4] = {k14.x, k14.y, k14.z, k14.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                nn[j] = next_cell(left[j], rg.ev[(ep[j] + 2) & (kEvRing - 1)], gmv[j], sdv[j], rsv[j], k1v[j], cc);
+            // ---- band placement (Suzuki-Kasahara), GPU/align_cuda.cl:394-430
+            const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
+            k0 += right ? 1 : 0;
+            e0 += right ? 0 : 1;
+            band_range(k0, e0, n_events, n_kmers, lo, hi);
+            // ---- skip candidate (exact), comparison
+            bool rare = false;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int o = (4 * lane + j - k0) & 127;
+                ep[j] = e0 - o;
+                valid[j] = (o >= lo) && (o < hi);
+                uint32_t from_du;
+                const float best_du = pick_du(nc[j].d, u[j], from_du);
+                bool okl;
+                const float l = exact_skip(left[j], cc.skip_h, cc.skip_l, okl);
+                best[j] = pick_l(best_du, from_du, l, from[j]);
+                bad[j] = valid[j] && !(nc[j].ok && oku[j] && okl);
+                rare |= bad[j];
+            }
+            if (__any_sync(kFull, rare)) {
+                to_slow = true;
+                break;
+            }
+            finish();
+        }
+        if (!to_slow) break;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (bad[j]) {  // a proof failed: the reference's FP64 arithmetic
+                const int sj = 4 * lane + j;
+                best[j] = cell_slow(LP[j], S1[j], left[j], rg.ev[ep[j] & (kEvRing - 1)], rg.gm[sj], rg.sd[sj],
+                                    rg.k1[sj], cc, from[j]);
+                ++slow;
+            }
+        }
+        finish();
+        ++b;
     }
     cp_async_wait_all();  // no copy may land in shared memory after the read is done
     __syncwarp();
@@ -371,161 +394,244 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 }
 
 // ---------------------------------------------------------------- wide shape
-// Eight warps per read.  Threads 0-127 ("band" threads) own slot t and run the
-// band-to-band critical path: up candidate, placement, skip candidate,
-// comparison, stores.  Threads 128-255 ("emission" threads) own slot t-128 and
-// compute, during band b, band b+1's emission and exact diagonal candidate,
-// handing them over in shared memory; they also run the prefetch rings.  One
-// barrier per band; every thread evaluates the band placement itself.
-struct WideSmem {
+// Sixteen warps per read in four groups of 128 threads; thread t of a group
+// works on slot t.  One barrier per band: B_b, once band b's scores are in shared
+// memory.  Between B_{b-1} and B_b:
+//   B  (warps 0-3)    band b only: the up candidate from this slot's own band
+//                     b-1 score, the end and left-neighbour cells of band b-1,
+//                     the placement, the exact skip candidate, the comparison
+//                     and the stores.  Everything else runs in the other groups,
+//                     so that B's loop body is one short block.
+//   D  (warps 4-7)    places band b too and prepares band b+1: the exact
+//                     diagonal candidate (from band b-1's left neighbour), which
+//                     cells lie inside the read and the band for either move,
+//                     and the trim cell's value.
+//   E0 (warps 8-11)   even b: band b+2's emissions and their exact splits, with
+//   E1 (warps 12-15)  odd b the k-mer assignment of band b-1 (a slot keeps its
+//                     k-mer for as long as it can be inside the band); the other
+//                     half does band b-1's bookkeeping (last k-mer column, band
+//                     origin, trace stores of four bands per 32-bit word).  E0
+//                     also runs the prefetch rings.
+struct alignas(16) WideSmem {
     Rings rg;
-    float sc[2][kSlots];  // band scores by slot, double buffered
-    float nd[2][kSlots];  // next band: exact diagonal candidate
-    float np[2][kSlots];  // next band: em + stay split (p, w) for the up candidate
-    float nw[2][kSlots];
-    float ne[2][kSlots];  // next band: emission
-    int32_t nok[2][kSlots];
+    float sc[2][kSlots];                       // band scores, buffer b & 1
+    float em[4][kSlots];                       // emission of band b, buffer b & 3
+    float pstep[4][kSlots], wstep[4][kSlots];  // em + step split
+    float pstay[4][kSlots], wstay[4][kSlots];  // em + stay split
+    float magu[4][kSlots];                     // |em| + |stay_h|; NaN when the division is not proven
+    float dc[2][kSlots];                       // exact diagonal candidate of band b
+    int32_t flags[2][kSlots];                  // band b: 1 inside if down, 2 inside if right, 4 d proven
+    float trim[2];                             // band b's trim cell value (-inf: outside the read)
+    uint32_t fr[8][kSlots];                    // backpointer of band b at [b & 7]
+    int32_t k0h[8];                            // lower-left k-mer of band b at [b & 7]
 };
 
-__device__ __forceinline__ void put_next(WideSmem& ws, int buf, int t, const NextCell& n) {
-    ws.nd[buf][t] = n.d;
-    ws.np[buf][t] = n.su.p;
-    ws.nw[buf][t] = n.su.w;
-    ws.ne[buf][t] = n.em;
-    ws.nok[buf][t] = n.ok ? 1 : 0;
+constexpr int kWideThreads = 512;
+
+// Named barrier 1 over the block: the groups reach it from different code
+// paths, once per band each.
+__device__ __forceinline__ void wide_barrier() { asm volatile("bar.sync 1, 512;\n" ::: "memory"); }
+
+// E: emission of slot t for the band whose event for this slot is e, into buffer
+// buf (band & 3: written two bands ahead while B reads the current band's).
+__device__ __forceinline__ void wide_emission(WideSmem& ws, const CellConsts& cc, int t, int buf, int e) {
+    bool ok;
+    const float em = emission_fast(ws.rg.ev[e & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t], ws.rg.rsd[t],
+                                   ws.rg.k1[t], ok);
+    const EmSplit s1 = em_split(em, cc.step_h, cc.step_l);
+    const EmSplit s2 = em_split(em, cc.stay_h, cc.stay_l);
+    ws.em[buf][t] = em;
+    ws.pstep[buf][t] = s1.p;
+    ws.wstep[buf][t] = s1.w;
+    ws.pstay[buf][t] = s2.p;
+    ws.wstay[buf][t] = s2.w;
+    ws.magu[buf][t] = ok ? __fadd_rn(fabsf(em), fabsf(cc.stay_h)) : __int_as_float(0x7fc00000);
 }
 
-__device__ __forceinline__ NextCell get_next(const WideSmem& ws, int buf, int t) {
-    NextCell n;
-    n.d = ws.nd[buf][t];
-    n.su.p = ws.np[buf][t];
-    n.su.w = ws.nw[buf][t];
-    n.em = ws.ne[buf][t];
-    n.ok = ws.nok[buf][t] != 0;
-    return n;
+// D: band bn's diagonal candidate from `diag`, its inside flags and trim value,
+// with the band before it placed at k0.
+__device__ __forceinline__ void wide_diag(WideSmem& ws, const CellConsts& cc, const GlobalConsts& g, int t, int bn,
+                                          float diag, int k0, int n_events, int n_kmers) {
+    const int buf = bn & 1, ebuf = bn & 3;
+    const float em = ws.em[ebuf][t];
+    const EmSplit s1{ws.pstep[ebuf][t], ws.wstep[ebuf][t]};
+    bool okd;
+    const float d = exact_from_split(diag, s1, __fadd_rn(fabsf(em), fabsf(cc.step_h)), fabsf(em) < INFINITY, okd);
+    const int o = (t - k0) & 127;
+    const int kk = k0 + o;
+    const int e = bn - 2 - kk;
+    const bool inb = (kk >= 0) && (kk < n_kmers) && (e >= 0) && (e < n_events);
+    const int f = ((inb && o < kBand) ? 1 : 0) | ((inb && o >= 1 && o <= kBand) ? 2 : 0) | (okd ? 4 : 0);
+    ws.dc[buf][t] = d;
+    ws.flags[buf][t] = f;
+    if (k0 <= 0 && t == 0) {
+        // trim cell of band bn (k = -1): event bn - 1, (float)(lp_trim * (e + 1)) (GPU/align_cuda.cl:431-443)
+        const int e_t = bn - 1;
+        ws.trim[buf] = (e_t < n_events) ? __double2float_rn(__dmul_rn(g.lp_trim, (double)(e_t + 1))) : -INFINITY;
+    }
 }
 
-constexpr int kWideThreads = 256;
+__device__ __forceinline__ bool band_moves_right(float ll, float ur, int b) {
+    // Suzuki-Kasahara (GPU/align_cuda.cl:394-430); both ends -inf: alternate
+    return (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
+}
 
-// Named barrier 1 over the 256 threads of a wide read: the band and emission
-// threads reach it from different code paths, once per band each.
-__device__ __forceinline__ void wide_barrier() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
-
-// Called by all 256 threads of a block.
+// Called by all 512 threads of a block.
 template <bool kScores>
 __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, int tid) {
     const CellConsts cc = make_consts(r, a.g);
     const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
-    const bool band_thread = tid < kSlots;
+    const int group = tid >> 7;  // 0 = B, 1 = D, 2 = E0, 3 = E1
     const int t = tid & (kSlots - 1);
-    const int ring_t = band_thread ? 1000 : t;  // emission threads run the rings
+    const int ring_t = group == 2 ? t : 1000;  // E0 runs the rings
 
-    int k0 = -1 - kBand / 2, e0 = kBand / 2;
+    int k0 = -1 - kBand / 2, e0 = kBand / 2;  // band 1 (band 0 is (49,-51), band 1 moved down)
     RingState rs;
     rings_init(ws.rg, rs, a, r, ring_t, k0, e0);
-    int ep = e0 - ((t - k0) & 127);  // my slot's event under the previous band's placement
-    if (band_thread) ws.sc[1][t] = (t == 127) ? a.g.trim_f : -INFINITY;
-    wide_barrier();
-    if (!band_thread) {
-        const float lp0 = (t == 0) ? 0.0f : -INFINITY;  // band 0 shifted by one slot
-        put_next(ws, 0, t, next_cell(lp0, ws.rg.ev[(ep + 1) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
-                                     ws.rg.rsd[t], ws.rg.k1[t], cc));
+    if (group == 0) {
+        ws.sc[1][t] = (t == 127) ? a.g.trim_f : -INFINITY;
+        ws.fr[0][t] = 0u;
+        ws.fr[1][t] = (t == 127) ? ABEA_FROM_U : 0u;
+    } else if (group == 1 && t == 0) {
+        ws.k0h[0] = k0;
+        ws.k0h[1] = k0;
+        a.band_k0[r.band_off] = k0;
     }
-    if (band_thread) {
-        // ------------------------------------------------ band threads
-        uint8_t* trace = a.trace + r.band_off * kSlots;
+    wide_barrier();
+    if (group >= 2) {
+        // bands 2 (E0) and 3 (E1) under band 1's k-mer assignment: event = band - 2 - k-mer
+        const int kk = k0 + ((t - k0) & 127);
+        const int bn = group == 2 ? 2 : 3;
+        wide_emission(ws, cc, t, bn & 3, bn - 2 - kk);
+    }
+    wide_barrier();
+    if (group == 0) {
+        // ------------------------------------------------ B: the critical path
         float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
-        int32_t* bk0 = a.band_k0 + r.band_off;
-        float* lastc = a.last_col + r.ev_off;
         float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // band 1
-        float lp = (t == 0) ? 0.0f : -INFINITY;
-        uint32_t tword = (t == 127) ? (ABEA_FROM_U << 8) : 0u;
-        int my_k0 = k0;
+        float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
         if (kScores) {
             scores[t] = (t == 127) ? 0.0f : -INFINITY;
             scores[kSlots + t] = s_prev;
         }
         unsigned long long slow = 0;
-        const int sl_last = (n_kmers - 1) & 127;
-        wide_barrier();
-        for (int b = 2; b < n_bands; ++b) {
-            const int pb = (b - 1) & 1;
-            const float ll = ws.sc[pb][k0 & 127];
-            const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
-            const float left = ws.sc[pb][(t + 127) & 127];
-            const NextCell nc = get_next(ws, b & 1, t);
-            bool oku;
-            const float u = cell_u(s_prev, nc, cc, oku);
-            const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
-            k0 += right ? 1 : 0;
-            e0 += right ? 0 : 1;
-            int lo, hi;
-            band_range(k0, e0, n_events, n_kmers, lo, hi);
-            const int o = (t - k0) & 127;
-            ep = e0 - o;
-            const bool valid = (o >= lo) && (o < hi);
-            uint32_t from;
-            bool need_l;
-            float best = cell_b(nc.d, u, left, cc, from, need_l);
-            bool bad = !(nc.ok && oku);
-            if (valid && (need_l || bad)) {
-                if (need_l) {
-                    bool ok;
-                    best = cell_l(nc.d, u, left, cc, from, ok);
-                    bad |= !ok;
-                }
-                if (bad) {
-                    best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
-                                     ws.rg.k1[t], cc, from);
-                    ++slow;
-                }
-            }
+        // Band state kept across the exit to the slow path.  A band in which a
+        // proof failed in any lane of the warp leaves the inner loop
+        // (warp-uniform) and is finished below with the reference's FP64
+        // arithmetic: the inner loop holds no division routine and no FP64 code.
+        int b = 2, cb = 0;
+        float best = 0.0f, left = 0.0f;
+        uint32_t from = 0u;
+        bool valid = false, bad = false;
+        auto finish = [&]() {
             best = valid ? best : -INFINITY;
             from = valid ? from : 0u;
-            const int ol = n_kmers - 1 - k0;
-            if (k0 <= -1 || ol < kBand) {  // trim cell (k = -1, slot 127); last k-mer column
-                if (t == 127 && k0 <= -1 && k0 >= -kBand) {
-                    const int e_t = e0 + 1 + k0;
-                    const bool in = e_t >= 0 && e_t < n_events;
-                    best = in ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
-                    from = in ? ABEA_FROM_U : 0u;
-                }
-                if (t == sl_last && ol >= lo && ol < hi) lastc[e0 - ol] = best;
-            }
-            ws.sc[b & 1][t] = best;
+            // trim cell (k = -1, slot 127) while the band still reaches below k-mer 0
+            const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
+            const float tv = ws.trim[cb];
+            best = here ? tv : best;
+            from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
+            ws.sc[cb][t] = best;
+            ws.fr[b & 7][t] = from;
+            if (kScores) scores[(int64_t)b * kSlots + t] = best;
             lp = left;
             s_prev = best;
-            tword |= from << (8 * (b & 3));
-            if ((b & 3) == 3 || b == n_bands - 1) {
-                reinterpret_cast<uint32_t*>(trace + (int64_t)(b >> 2) * 512)[t] = tword;
-                tword = 0u;
+        };
+        while (true) {
+            bool to_slow = false;
+            for (; b < n_bands; ++b) {
+                wide_barrier();  // B_{b-1}
+                const int pb = (b - 1) & 1;
+                cb = b & 1;
+                const float ll = ws.sc[pb][k0 & 127];
+                const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
+                left = ws.sc[pb][(t + 127) & 127];
+                const float d = ws.dc[cb][t];
+                const int f = ws.flags[cb][t];
+                const EmSplit su{ws.pstay[b & 3][t], ws.wstay[b & 3][t]};
+                const float mu = ws.magu[b & 3][t];
+                // up candidate from this slot's own band b-1 score
+                bool oku;
+                const float u = exact_from_split(s_prev, su, mu, mu < INFINITY, oku);
+                const bool right = band_moves_right(ll, ur, b);
+                k0 += right ? 1 : 0;
+                e0 += right ? 0 : 1;
+                valid = (f & (right ? 2 : 1)) != 0;
+                // d vs u (U wins ties), then the skip candidate (L wins ties)
+                uint32_t from_du;
+                const float best_du = pick_du(d, u, from_du);
+                bool okl;
+                const float l = exact_skip(left, cc.skip_h, cc.skip_l, okl);
+                best = pick_l(best_du, from_du, l, from);
+                bad = valid && !(oku && okl && (f & 4));
+                if (__any_sync(kFull, bad)) {
+                    to_slow = true;
+                    break;
+                }
+                finish();
             }
-            if (kScores) scores[(int64_t)b * kSlots + t] = best;
-            my_k0 = ((b & 127) == t) ? k0 : my_k0;
-            if ((b & 127) == 127 || b == n_bands - 1) {
-                if (t <= (b & 127)) bk0[(b & ~127) + t] = my_k0;
+            if (!to_slow) break;
+            if (bad) {  // a proof failed: the reference's FP64 arithmetic
+                const int ep = e0 - ((t - k0) & 127);
+                best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
+                                 ws.rg.k1[t], cc, from);
+                ++slow;
             }
-            wide_barrier();
+            finish();
+            ++b;
         }
+        wide_barrier();  // B_{n_bands-1}
         if (slow) atomicAdd(&a.counters[0], slow);
-    } else {
-        // ------------------------------------------------ emission threads
-        wide_barrier();
+    } else if (group == 1) {
+        // ------------------------------------------------ D
+        wide_diag(ws, cc, a.g, t, 2, (t == 0) ? 0.0f : -INFINITY, k0, n_events, n_kmers);
         for (int b = 2; b < n_bands; ++b) {
+            wide_barrier();  // B_{b-1}
             const int pb = (b - 1) & 1;
             const float ll = ws.sc[pb][k0 & 127];
             const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
-            const float left = ws.sc[pb][(t + 127) & 127];
-            // band b+1: event two past the slot's event under band b-1's placement
-            const NextCell nn = next_cell(left, ws.rg.ev[(ep + 2) & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
-                                          ws.rg.rsd[t], ws.rg.k1[t], cc);
-            put_next(ws, (b + 1) & 1, t, nn);
-            const bool right = (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
+            const bool right = band_moves_right(ll, ur, b);
             k0 += right ? 1 : 0;
-            e0 += right ? 0 : 1;
-            ep = e0 - ((t - k0) & 127);
-            if ((b & 3) == 3) rings_step(ws.rg, rs, a, r, ring_t, k0, e0, 7);
-            wide_barrier();
+            if (t == 0) ws.k0h[b & 7] = k0;
+            if (b + 1 < n_bands)
+                wide_diag(ws, cc, a.g, t, b + 1, ws.sc[pb][(t + 127) & 127], k0, n_events, n_kmers);
+        }
+        wide_barrier();  // B_{n_bands-1}
+    } else {
+        // ------------------------------------------------ E0 / E1
+        const int half = group - 2;
+        uint8_t* trace = a.trace + r.band_off * kSlots;
+        int32_t* bk0 = a.band_k0 + r.band_off;
+        float* lastc = a.last_col + r.ev_off;
+        const int sl_last = (n_kmers - 1) & 127;
+        for (int b = 2; b <= n_bands; ++b) {
+            wide_barrier();  // B_{b-1}
+            const int bp = b - 1;
+            const int kp = ws.k0h[bp & 7];  // band b-1's placement
+            if ((b & 1) == half) {
+                // band b+2's emissions under band b-1's k-mer assignment
+                if (b + 2 < n_bands) wide_emission(ws, cc, t, (b + 2) & 3, b - (kp + ((t - kp) & 127)));
+                if (half == 0 && (b & 3) == 2) rings_step(ws.rg, rs, a, r, ring_t, kp, bp - 2 - kp, 9);
+            } else {
+                // band b-1's bookkeeping
+                const int ep0 = bp - 2 - kp;
+                const int ol = n_kmers - 1 - kp;
+                if (ol < kBand && t == sl_last && bp >= 2) {  // last k-mer column (GPU/align_cuda.cl:722-746)
+                    int lo, hi;
+                    band_range(kp, ep0, n_events, n_kmers, lo, hi);
+                    if (ol >= lo && ol < hi) lastc[ep0 - ol] = ws.sc[bp & 1][t];
+                }
+                if (t == 0) bk0[bp] = kp;
+                if ((bp & 3) == 3 || bp == n_bands - 1) {
+                    // four bands of backpointers, byte j = band 4q + j (bands past the read: 0)
+                    const int q0 = bp & ~3, nj = bp - q0;
+                    uint32_t word = 0u;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (j <= nj) word |= (ws.fr[(q0 + j) & 7][t] & 0xffu) << (8 * j);
+                    reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
+                }
+            }
         }
     }
     cp_async_wait_all();
@@ -533,7 +639,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
 }
 
 // ---------------------------------------------------------------- post
-struct PostSmem {
+struct alignas(16) PostSmem {
     uint8_t tr[2][kPostChunkBands * kSlots];
 };
 
@@ -805,9 +911,14 @@ struct BatchedSmem {
     PostSmem post[kBatchedWarps];      // every warp's post staging
     int32_t pick;
 };
+static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSmem, post) % 16 == 0 &&
+                  sizeof(Rings) % 16 == 0 && sizeof(PostSmem) % 16 == 0,
+              "cp.async destinations must be 16-byte aligned");
+static_assert(sizeof(BatchedSmem) <= 227 * 1024, "batched kernel shared memory exceeds the per-block limit");
+
 
 template <bool kScores>
-__global__ void __launch_bounds__(kWideThreads) abea_batched_kernel(CoreArgs a, PostArgs p) {
+__global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs a, PostArgs p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchedSmem& sm = *reinterpret_cast<BatchedSmem*>(smem_raw);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;

@@ -4,6 +4,7 @@
 // For pseudo-random and adversarial inputs it compares
 //   div_fast(n, sd, RN(1/sd))          with __fdiv_rn(n, sd)
 //   exact_sum(a, bh, bl, c)            with RN32(RN64(RN64(a + B) + c))
+//   exact_skip(a, bh, bl)              with RN32(RN64(a + B))
 // and counts the cases where the fast routine claims success but differs
 // (must be zero) and the cases where it declines (the kernels then fall back).
 // Adversarial sums are built around float rounding midpoints, where double
@@ -72,12 +73,32 @@ __global__ void selftest_kernel(uint64_t seed, int iters, unsigned long long* co
         float r = __double2float_rn(__dadd_rn(__dadd_rn((double)a, B), (double)c));
         if (ok && __float_as_int(v) != __float_as_int(r)) ++c2;
         if (!ok) ++c3;
+        // ---- the skip candidate a + B: f5c's lp_skip or the random B; random a,
+        // or a aimed so that a + B lands next to a float rounding midpoint
+        {
+            const double bs = (it & 4) ? -23.025850929940457 : B;
+            float as;
+            if (it & 8) {
+                as = -(float)(50000.0 * (double)unit(s)) - 31.0f;
+            } else {
+                const float a0 = -(float)(20000.0 * (double)unit(s)) - 31.0f;
+                const float s1 = __double2float_rn((double)a0 + bs);
+                const float nb = nextafterf(s1, (unit(s) < 0.5f) ? 0.0f : -INFINITY);
+                const double m = 0.5 * ((double)s1 + (double)nb);
+                as = __double2float_rn(m - bs);
+            }
+            const float bhs = (float)bs, bls = (float)(bs - (double)bhs);
+            const float vs = exact_skip(as, bhs, bls, ok);
+            const float rs = __double2float_rn(__dadd_rn((double)as, bs));
+            if (ok && __float_as_int(vs) != __float_as_int(rs)) ++c2;
+            if (!ok) ++c3;
+        }
     }
     atomicAdd(&counters[0], c0);
     atomicAdd(&counters[1], c1);
     atomicAdd(&counters[2], c2);
     atomicAdd(&counters[3], c3);
-    atomicAdd(&counters[4], (unsigned long long)iters);
+    atomicAdd(&counters[4], (unsigned long long)iters);  // per kind (the sums count two per case)
 }
 
 }  // namespace abea

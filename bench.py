@@ -259,6 +259,54 @@ def run_mode(pkg, batch, mode, device, steps, warmup, autotune=False):
     return res
 
 
+def adjoint_report(pkg, synth, device, seed):
+    """The adjoint workload: 4,096 reads U(1 kb, 10 kb) whose scalings are off
+    by U(-8, 8) pA and a factor U(0.9, 1.1): forward + backward throughput, and the
+    scalings recovered by three annealed Gauss-Newton rounds."""
+    b = synth.make_batch("adjoint", seed=seed, perturb=True)
+    true = b.meta["true_scalings"]
+    ctx = pkg.Context(device, pkg.MODE_BATCHED)
+    ctx.set_option(pkg.OPT_VAR_AWARE, 1)
+    dev = ctx.upload(b)
+    dev.run()
+    dev.sync()
+    fwd, bwd = [], []
+    for _ in range(3):
+        ctx.flush_l2()
+        ctx.mark(0)
+        dev.run()
+        ctx.mark(1)
+        fwd.append(ctx.elapsed(0, 1))
+        t0 = time.perf_counter()
+        g = dev.backward()
+        bwd.append((time.perf_counter() - t0) * 1e3)
+    n_grad = int(np.count_nonzero(g["status"] == 0))
+
+    def err(sc):
+        ds = np.abs(sc["shift"].astype(np.float64) - true["shift"])
+        dk = np.abs(sc["scale"].astype(np.float64) / true["scale"] - 1.0)
+        return {"shift_pA_median": float(np.median(ds)), "shift_pA_p90": float(np.percentile(ds, 90)),
+                "scale_rel_median": float(np.median(dk)), "scale_rel_p90": float(np.percentile(dk, 90)),
+                "within_1pA_1pct": float(np.mean((ds < 1.0) & (dk < 0.01)))}
+
+    before = err(b.scalings)
+    t0 = time.perf_counter()
+    sc = dev.recalibrate(3, first_temperature=5.0)
+    t_gn = time.perf_counter() - t0
+    cells = b.band_cells()
+    dev.close()
+    ctx.close()
+    return {
+        "workload": "4096 reads U(1 kb, 10 kb); scalings perturbed by shift U(-8, 8) pA, scale x U(0.9, 1.1)",
+        "emission": "var-aware (stdv*var, log stdv + log var)",
+        "forward_ms": statistics.mean(fwd), "forward_band_cells_per_s": cells / (statistics.mean(fwd) / 1e3),
+        "backward_ms_incl_d2h": statistics.mean(bwd), "reads_with_gradient": n_grad, "reads": b.n_reads,
+        "gauss_newton": {"iterations": 3, "first_temperature": 5.0, "wall_s": t_gn,
+                         "error_before": before, "error_after": err(sc)},
+        "checked_in_tests": "FP64 oracle gradient and central differences h=1e-3 (tests/test_adjoint.py)",
+    }
+
+
 def ours(args, dist):
     pkg = load_package()
     from abea_gb300 import synth
@@ -360,6 +408,8 @@ def ours(args, dist):
         un["batched_over_plain"] = un["batched"]["value"] / un["plain"]["value"]
         un["workload"] = WORKLOADS["uneven"]
         out["uneven"] = un
+    if args.compare and dist.world == 1:
+        out["adjoint"] = adjoint_report(pkg, synth, device, args.seed)
     if args.cpu and dist.world == 1:
         threads = os.cpu_count() or 1
         t = cpu_align(batch, threads)
