@@ -70,12 +70,35 @@ __device__ __forceinline__ float div_fast(float n, float sd, float rsd, bool& ok
     return hp;
 }
 
+// Division n/sd rounded to nearest from rsd = RN(1/sd): q0 = RN(n*rsd), the
+// exact remainder r = n - sd*q0 by FMA, and q = RN(q0 + r*rsd), which is RN(n/sd)
+// by Markstein's theorem (IBM J. Res. Dev. 34, 1990; Cornea-Hasegan, Golliver
+// and Markstein, ARITH-14, 1999) when rsd is the correctly rounded reciprocal
+// and nothing under- or overflows.  ok = false outside 2^-100 <= |q0| <= 2^100
+// (n = 0 excepted) or when rsd is not a finite positive number.
+constexpr float kHuge = 1.2676506002282294e30f;  // 2^100
+__device__ __forceinline__ float div_rn(float n, float sd, float rsd, bool& ok) {
+    const float q0 = __fmul_rn(n, rsd);
+    const float r = __fmaf_rn(-q0, sd, n);
+    const float q = __fmaf_rn(r, rsd, q0);
+    const float aq = fabsf(q0);
+    ok = ((aq >= kTiny && aq <= kHuge) || n == 0.0f) && rsd > 0.0f && rsd < INFINITY;
+    return q;
+}
+
 // log_normal_pdf of the reference in its operation order
 // (GPU/align_cuda.cl:68-75, 511-528): a = (x - mean)/stdv;
 // lp = (log_inv_sqrt_2pi - log_stdv) + ((-0.5f*a)*a); k1 is the first bracket,
 // precomputed per k-mer with the same rounding.
 __device__ __forceinline__ float emission_fast(float x, float gm, float sd, float rsd, float k1, bool& ok) {
     float a = div_fast(__fsub_rn(x, gm), sd, rsd, ok);
+    float t = __fmul_rn(__fmul_rn(-0.5f, a), a);
+    return __fadd_rn(k1, t);
+}
+
+// emission_fast with div_rn: no bracket, one FMA fewer.
+__device__ __forceinline__ float emission_rn(float x, float gm, float sd, float rsd, float k1, bool& ok) {
+    float a = div_rn(__fsub_rn(x, gm), sd, rsd, ok);
     float t = __fmul_rn(__fmul_rn(-0.5f, a), a);
     return __fadd_rn(k1, t);
 }

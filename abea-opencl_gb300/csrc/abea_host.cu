@@ -528,7 +528,7 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
     la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
                        b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
                        b->d_slow, b->d_order, b->d_queue, b->n_wide};
-    la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1,
+    la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1, b->d_km_rsd,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
                        b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event};
     la.sm_count = c->sm_count;

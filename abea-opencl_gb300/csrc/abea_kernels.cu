@@ -40,7 +40,7 @@
 namespace abea {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kPostChunkBands = 32;  // trace bands staged per shared-memory chunk in post
+constexpr int kPostChunkBands = 16;  // trace bands per chunk of post's four-chunk shared-memory ring
 
 __host__ __device__ __forceinline__ int round_up_dev(int x) { return (x + kChunk - 1) & ~(kChunk - 1); }
 
@@ -51,6 +51,7 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_group1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 __device__ __forceinline__ float sel4(const float (&v)[4], int j) {
     float r = v[0];
@@ -640,7 +641,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
 
 // ---------------------------------------------------------------- post
 struct alignas(16) PostSmem {
-    uint8_t tr[2][kPostChunkBands * kSlots];
+    uint8_t tr[4 * kPostChunkBands * kSlots];  // ring of 64 bands of trace, tile layout
 };
 
 __device__ __forceinline__ float path_emission(const PostArgs& a, const ReadDesc& r, int k, int e) {
@@ -725,52 +726,75 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
 
     if (best > -INFINITY) {
         // A finite end: the path only visits computed cells.  Walked by lane 0
-        // over shared-memory chunks of 32 bands, the next chunk in flight.
+        // over a shared-memory ring of four 16-band chunks of the trace (band B
+        // at ring band B & 63, the global tile layout): the chunk being walked
+        // and the one below it are resident, the two below those in flight.
+        // Each walk iteration loads the bytes of the current cell and of its
+        // three possible predecessors at once and takes two steps; the moves are
+        // decoded arithmetically (D = 0, U = 1, L = 2: the k-mer steps back
+        // unless U, the event unless L).
         int cur_e = best_e, cur_k = n_kmers - 1, gap = 0;
-        int chunk_lo = ((cur_e + cur_k + 2) / kPostChunkBands) * kPostChunkBands;
         const int bands_pad = (n_bands + 3) & ~3;
-        int buf = 0;
-        auto stage = [&](int lo_band, int which) {
-            const int bytes = min(kPostChunkBands, bands_pad - lo_band) * kSlots;
-            const uint8_t* src = trace + (int64_t)lo_band * kSlots;
-            for (int off = lane * 16; off < bytes; off += 32 * 16) cp_async16(&sm.tr[which][off], src + off);
-            cp_async_commit();
+        auto stage = [&](int c) {  // chunk c = bands [16c, 16c + 16)
+            if (c >= 0) {
+                const int lo_band = c * kPostChunkBands;
+                const int bytes = min(kPostChunkBands, bands_pad - lo_band) * kSlots;
+                const uint8_t* src = trace + (int64_t)lo_band * kSlots;
+                uint8_t* dst = sm.tr + (c & 3) * (kPostChunkBands * kSlots);
+                for (int off = lane * 16; off < bytes; off += 32 * 16) cp_async16(dst + off, src + off);
+            }
+            cp_async_commit();  // an empty group keeps the group count in step
         };
-        stage(chunk_lo, buf);
+        const uint8_t* tb = sm.tr;
+        auto T = [&](int band, int k) -> uint32_t {  // 0, 1 or 2; the clamp keeps every step a move
+            const int rb = band & 63;
+            return min((uint32_t)tb[((rb >> 2) << 9) | ((k & 127) << 2) | (rb & 3)], 2u);
+        };
+        int c = (cur_e + cur_k + 2) / kPostChunkBands;
+        stage(c);
+        stage(c - 1);
+        stage(c - 2);
         bool done = false;
-        while (!done) {
-            cp_async_wait_all();
+        for (; c >= 0 && !done; --c) {
+            cp_async_wait_group1();  // chunks c and c-1 have landed; c-2 may be in flight
             __syncwarp();
-            const int next_lo = chunk_lo - kPostChunkBands;
-            if (next_lo >= 0) stage(next_lo, buf ^ 1);
+            stage(c - 3);  // into the ring slot of chunk c+1, already walked
             if (lane == 0) {
-                const uint8_t* tb = sm.tr[buf];
-                int lb = cur_e + cur_k + 2 - chunk_lo, slot = cur_k & 127;
+                const int lo = c * kPostChunkBands;
+                int k = cur_k, e = cur_e;
                 while (true) {
-                    if ((cur_k | cur_e) < 0) {
-                        done = true;
-                        break;
-                    }
-                    if (lb < 0) break;
-                    if (n_out < cap) out[n_out] = abea_aligned_pair_t{cur_k, cur_e};
+                    const int band = e + k + 2;
+                    if (((k | e) < 0) || band < lo) break;
+                    // this cell (band >= 2) and its predecessors (bands >= lo - 2: resident)
+                    const uint32_t f0 = T(band, k), fu = T(band - 1, k);
+                    const uint32_t fl = T(band - 1, k - 1), fd = T(band - 2, k - 1);
+                    // step 1 from (k, e)
+                    if (n_out < cap) out[n_out] = abea_aligned_pair_t{k, e};
                     ++n_out;
-                    last_k = cur_k;
-                    const uint32_t from = tb[((lb >> 2) << 9) | (slot << 2) | (lb & 3)];
-                    last_from = (int)from;
-                    // D: band-2, slot-1; U: band-1, same slot; L: band-1, slot-1
-                    const bool is_u = from == ABEA_FROM_U, is_l = from == ABEA_FROM_L;
-                    lb -= (is_u || is_l) ? 1 : 2;
-                    slot = is_u ? slot : ((slot - 1) & 127);
-                    cur_k -= is_u ? 0 : 1;
-                    cur_e -= is_l ? 0 : 1;
-                    gap = is_l ? gap + 1 : 0;
+                    last_k = k;
+                    last_from = (int)f0;
+                    gap = (f0 == ABEA_FROM_L) ? gap + 1 : 0;
                     max_gap = max(max_gap, gap);
+                    const int k1 = k - (int)((f0 & 1u) ^ 1u), e1 = e - (int)((f0 >> 1) ^ 1u);
+                    const uint32_t f1 = ((fd | (fu << 8) | (fl << 16)) >> (8 * f0)) & 0xffu;
+                    k = k1;
+                    e = e1;
+                    if ((k1 | e1) < 0) break;
+                    // step 2 from (k1, e1): its byte was loaded with step 1's
+                    if (n_out < cap) out[n_out] = abea_aligned_pair_t{k1, e1};
+                    ++n_out;
+                    last_k = k1;
+                    last_from = (int)f1;
+                    gap = (f1 == ABEA_FROM_L) ? gap + 1 : 0;
+                    max_gap = max(max_gap, gap);
+                    k = k1 - (int)((f1 & 1u) ^ 1u);
+                    e = e1 - (int)((f1 >> 1) ^ 1u);
                 }
+                cur_k = k;
+                cur_e = e;
+                done = (k | e) < 0;
             }
             done = __shfl_sync(kFull, (int)done, 0) != 0;
-            chunk_lo = next_lo;
-            buf ^= 1;
-            if (chunk_lo < 0) done = true;
         }
         cp_async_wait_all();
         __syncwarp();
@@ -814,19 +838,23 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
             // Every emission with 0.5 <= |em| < 2^20 is a multiple of 2^-24; when the
             // magnitudes sum below 2^53 * 2^-24 all of the reference's partial double
             // sums are exact and equal this integer sum, whatever the order.
+            // The division is Markstein's (div_rn): no routine call, so that the
+            // loads of four cells are in flight at once.
             long long isum = 0, iabs = 0;
             bool exact = true;
+#pragma unroll 4
             for (int i2 = lane; i2 < n_out; i2 += 32) {
                 const abea_aligned_pair_t p = out[i2];
-                const float em = path_emission(a, r, p.ref_pos, p.read_pos);
+                const int64_t ko = r.km_off + p.ref_pos;
+                bool ok;
+                const float em = emission_rn(a.ev_mean[r.ev_off + p.read_pos], a.km_gm[ko], a.km_sd[ko], a.km_rsd[ko],
+                                             a.km_k1[ko], ok);
                 const float aem = fabsf(em);
-                if (aem >= 0.5f && aem < 1048576.0f) {
-                    const long long q = __float2ll_rn(__fmul_rn(em, 16777216.0f));
-                    isum += q;
-                    iabs += q < 0 ? -q : q;
-                } else {
-                    exact = false;
-                }
+                const long long q = __float2ll_rn(__fmul_rn(em, 16777216.0f));
+                const bool in = ok && aem >= 0.5f && aem < 1048576.0f;
+                isum += in ? q : 0ll;
+                iabs += in ? (q < 0 ? -q : q) : 0ll;
+                exact = exact && in;
             }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
@@ -1117,7 +1145,7 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     PreArgs pre{d_desc, 1, g, sequence, events, model, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col};
     CoreArgs core{d_desc, 1, g, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col, trace, nullptr, band_k0,
                   counters, nullptr, nullptr, 0};
-    PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, last_col, trace, band_k0, pairs, n_pairs, best, status};
+    PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, km_rsd, last_col, trace, band_k0, pairs, n_pairs, best, status};
     abea_pre_kernel<<<1, 128, 0, st>>>(pre);
     abea_core_warp_kernel<false><<<1, 32, 0, st>>>(core);
     abea_post_kernel<<<1, 32, 0, st>>>(post);

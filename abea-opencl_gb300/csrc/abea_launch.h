@@ -53,6 +53,7 @@ struct PostArgs {
     const float* km_gm;
     const float* km_sd;
     const float* km_k1;
+    const float* km_rsd;
     const float* last_col;
     const uint8_t* trace;
     const int32_t* band_k0;

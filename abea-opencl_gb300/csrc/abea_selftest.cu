@@ -3,6 +3,7 @@
 //
 // For pseudo-random and adversarial inputs it compares
 //   div_fast(n, sd, RN(1/sd))          with __fdiv_rn(n, sd)
+//   div_rn(n, sd, RN(1/sd))            with __fdiv_rn(n, sd)
 //   exact_sum(a, bh, bl, c)            with RN32(RN64(RN64(a + B) + c))
 //   exact_skip(a, bh, bl)              with RN32(RN64(a + B))
 // and counts the cases where the fast routine claims success but differs
@@ -48,6 +49,10 @@ __global__ void selftest_kernel(uint64_t seed, int iters, unsigned long long* co
         float q = div_fast(n, sd, __frcp_rn(sd), ok);
         float ref = __fdiv_rn(n, sd);
         if (ok && __float_as_int(q) != __float_as_int(ref)) ++c0;
+        if (!ok) ++c1;
+        // Markstein's form (div_rn): counted with the division
+        float q2 = div_rn(n, sd, __frcp_rn(sd), ok);
+        if (ok && __float_as_int(q2) != __float_as_int(ref)) ++c0;
         if (!ok) ++c1;
         // ---- sums: a + B + c with B a double constant
         double B;
