@@ -80,10 +80,15 @@ struct abea_batch {
     float min_lsd = 0.0f;        // smallest cached log stdv of the model
     std::vector<ReadDesc> reads;
     std::vector<int32_t> order;  // longest first
+    std::vector<int32_t> dev_order;       // the batched form's order: wide reads, then the rest longest first
+    std::vector<int32_t> dev_order_sent;  // the order last copied to the device
     int32_t n_wide = 0;          // leading reads of `order` run on the wide shape
     // sizes
     int64_t seq_bytes = 0, n_events_total = 0, ev_pad_total = 0, km_pad_total = 0,
             band_pad_total = 0, pair_cap = 0, band_cells = 0;
+    int64_t trace_pad_total = 0;  // bands of kept traces
+    int64_t ck_floats = 0;        // checkpoint records
+    int32_t n_ck = 0;             // checkpointed reads (recompute scratch slots)
     // device pointers (sub-ranges of the slab)
     DevSlab slab;
     ReadDesc* d_reads = nullptr;
@@ -94,6 +99,8 @@ struct abea_batch {
           *d_km_k1 = nullptr, *d_last_col = nullptr;
     uint8_t* d_trace = nullptr;
     float* d_scores = nullptr;
+    float* d_ck = nullptr;           // checkpoint records
+    uint8_t* d_ck_scratch = nullptr; // one kCkBands-band trace segment per checkpointed read
     int32_t* d_band_k0 = nullptr;
     abea_aligned_pair_t* d_pairs = nullptr;
     int32_t* d_n_pairs = nullptr;
@@ -121,6 +128,7 @@ struct abea_ctx {
     int64_t long_read_bands = 0;
     int64_t spin_limit = 1 << 22;
     int64_t var_aware = 0;
+    int64_t trace_budget = 0;  // bytes of trace a read may keep (0 = every trace)
     int sm_count = 0;
     cudaEvent_t ev[8] = {};
     cudaEvent_t marker[16] = {};
@@ -207,6 +215,10 @@ extern "C" abea_status_t abea_ctx_set_option(abea_ctx_t* c, abea_option_t opt, i
         c->spin_limit = v;
         return ABEA_OK;
     case ABEA_OPT_VAR_AWARE: c->var_aware = v != 0; return ABEA_OK;
+    case ABEA_OPT_TRACE_BUDGET:
+        if (v < 0) return fail(ABEA_ERR_INVALID_ARG, "trace budget must be >= 0");
+        c->trace_budget = v;
+        return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -220,6 +232,7 @@ extern "C" abea_status_t abea_ctx_get_option(abea_ctx_t* c, abea_option_t opt, i
     case ABEA_OPT_LONG_READ_BANDS: *v = c->long_read_bands; return ABEA_OK;
     case ABEA_OPT_SPIN_LIMIT: *v = c->spin_limit; return ABEA_OK;
     case ABEA_OPT_VAR_AWARE: *v = c->var_aware; return ABEA_OK;
+    case ABEA_OPT_TRACE_BUDGET: *v = c->trace_budget; return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -324,13 +337,14 @@ static int model_nonpos(float min_lsd, float log_var, int var_aware) {
     return k1 <= 0.0f ? 1 : 0;
 }
 
-static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware) {
+static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, int64_t trace_budget) {
     b->n_reads = in.n_reads;
     b->var_aware = var_aware;
     const float min_lsd = in.n_reads > 0 ? model_min_log_stdv(in.model) : 0.0f;
     b->min_lsd = min_lsd;
     b->reads.assign((size_t)in.n_reads, ReadDesc{});
-    int64_t seq_end = 0, ev_end = 0, km = 0, ev = 0, bands = 0, cells = 0;
+    int64_t seq_end = 0, ev_end = 0, km = 0, ev = 0, bands = 0, cells = 0, tbands = 0, ckf = 0;
+    int32_t n_ck = 0;
     for (int32_t i = 0; i < in.n_reads; ++i) {
         ReadDesc& r = b->reads[(size_t)i];
         int32_t len = in.read_len[i], ne = in.n_events[i];
@@ -353,6 +367,7 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware) {
             r.ev_off = ev;
             r.km_off = km;
             r.band_off = bands;
+            r.trace_off = tbands;
             continue;
         }
         r.n_bands = ne + nk + 2;
@@ -367,6 +382,17 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware) {
         r.ev_off = ev;
         r.km_off = km;
         r.band_off = bands;
+        // a trace over the budget: checkpoints every kCkBands bands instead
+        const int64_t trace_bytes = round_up(r.n_bands, 4) * (int64_t)kSlots;
+        r.ck = (trace_budget > 0 && trace_bytes > trace_budget) ? 1 : 0;
+        r.trace_off = tbands;
+        if (r.ck) {
+            r.ck_off = ckf;
+            r.ck_slot = n_ck++;
+            ckf += (int64_t)(r.n_bands / kCkBands + 1) * kCkStride;
+        } else {
+            tbands += round_up(r.n_bands, 4);
+        }
         ev += round_up(ne, kChunk);
         km += round_up(nk, kChunk);
         bands += round_up(r.n_bands, 4);
@@ -377,6 +403,9 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware) {
     b->ev_pad_total = ev;
     b->km_pad_total = km;
     b->band_pad_total = bands;
+    b->trace_pad_total = tbands;
+    b->ck_floats = ckf;
+    b->n_ck = n_ck;
     b->pair_cap = 2 * ev_end;
     b->band_cells = cells;
     // longest first; ties by index
@@ -393,7 +422,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Carves the device slab; grows it when needed.
 static abea_status_t ensure_device(abea_batch* b, bool scores) {
     size_t n = (size_t)std::max(b->n_reads, 1);
-    size_t sizes[29] = {
+    size_t sizes[31] = {
         sizeof(ReadDesc) * n,                                   // reads
         (size_t)std::max<int64_t>(b->seq_bytes, 1),             // seq
         sizeof(abea_event_t) * (size_t)std::max<int64_t>(b->n_events_total, 1),
@@ -404,7 +433,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // k1
         sizeof(float) * (size_t)std::max<int64_t>(b->ev_pad_total, 16),  // last_col
         sizeof(float) * (size_t)std::max<int64_t>(b->km_pad_total, 16),  // rsd
-        (size_t)kSlots * (size_t)std::max<int64_t>(b->band_pad_total, 4), // trace
+        (size_t)kSlots * (size_t)std::max<int64_t>(b->trace_pad_total, 4), // trace
         scores ? sizeof(float) * kSlots * (size_t)std::max<int64_t>(b->band_pad_total, 4) : 0,
         sizeof(int32_t) * (size_t)std::max<int64_t>(b->band_pad_total, 4),  // band_k0
         sizeof(abea_aligned_pair_t) * (size_t)std::max<int64_t>(b->pair_cap, 1),
@@ -422,8 +451,10 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         sizeof(double) * 5 * n,  // gn
         sizeof(double) * n,      // path_em
         sizeof(double) * 2 * ABEA_NUM_KMER,  // grad_model
+        sizeof(float) * (size_t)std::max<int64_t>(b->ck_floats, 16),  // checkpoints
+        (size_t)kCkBands * kSlots * (size_t)std::max<int32_t>(b->n_ck, 0),  // recompute scratch
         0};
-    const int n_bufs = 28;
+    const int n_bufs = 30;
     size_t total = 0;
     for (int i = 0; i < n_bufs; ++i) total += align256(sizes[i]);
     if (total > b->slab.bytes) {
@@ -439,7 +470,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
         b->slab.bytes = total;
     }
     char* p = (char*)b->slab.base;
-    void* ptrs[29];
+    void* ptrs[31];
     for (int i = 0; i < n_bufs; ++i) {
         ptrs[i] = sizes[i] ? (void*)p : nullptr;
         p += align256(sizes[i]);
@@ -472,6 +503,8 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
     b->d_gn = (double*)ptrs[25];
     b->d_path_em = (double*)ptrs[26];
     b->d_grad_model = (double*)ptrs[27];
+    b->d_ck = (float*)ptrs[28];
+    b->d_ck_scratch = (uint8_t*)ptrs[29];
     b->scores_kept = scores;
     return ABEA_OK;
 }
@@ -489,6 +522,7 @@ static abea_status_t upload(abea_batch* b, const HostInputs& in, cudaStream_t st
                              cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(b->d_order, b->order.data(), sizeof(int32_t) * b->order.size(),
                              cudaMemcpyHostToDevice, st));
+    b->dev_order_sent = b->order;
     return ABEA_OK;
 }
 
@@ -502,21 +536,27 @@ static int64_t d2h_bytes(const abea_batch* b) {
     return (int64_t)sizeof(abea_aligned_pair_t) * b->pair_cap + (int64_t)sizeof(int32_t) * b->n_reads;
 }
 
-// Reads of the batched form that run on the wide (4-warp) shape: the longest
-// reads whose band count exceeds what one warp would carry if the whole batch
-// were spread evenly over the resident warps (their warp-shape fill would
-// outlast the rest of the batch), at most one per resident block.
-static int choose_wide_reads(const abea_batch* b, int sm_count, int64_t threshold, bool scores) {
+// Reads of the batched form that run on the wide shape: the longest reads whose
+// band count exceeds what one warp would carry if the whole batch were spread
+// evenly over the resident warps (their warp-shape fill would outlast the rest
+// of the batch), at most one per resident block, never a checkpointed read.
+// Fills b->dev_order with those reads first, then the rest longest first.
+static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, bool scores) {
     const int blocks = batched_blocks_per_sm(scores) * sm_count;
     int64_t total = 0;
     for (const ReadDesc& r : b->reads) total += r.n_bands;
     if (threshold <= 0) threshold = std::max<int64_t>(1, total / std::max(1, blocks * 8));
-    int n = 0;
+    std::vector<int32_t> wide, rest;
     for (int32_t i : b->order) {
-        if (n >= blocks || b->reads[(size_t)i].n_bands < threshold) break;
-        ++n;
+        const ReadDesc& r = b->reads[(size_t)i];
+        if ((int)wide.size() < blocks && !r.ck && r.n_bands >= threshold)
+            wide.push_back(i);
+        else
+            rest.push_back(i);
     }
-    return n;
+    b->dev_order = wide;
+    b->dev_order.insert(b->dev_order.end(), rest.begin(), rest.end());
+    return (int)wide.size();
 }
 
 // Queues pre, core and post for a batch on the context's stream.
@@ -527,7 +567,7 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
                      b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col};
     la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
                        b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
-                       b->d_slow, b->d_order, b->d_queue, b->n_wide};
+                       b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch};
     la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1, b->d_km_rsd,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
                        b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event};
@@ -577,6 +617,12 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
             if (it != c->tuned.end()) thr = it->second;
         }
         b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept);
+        if (b->dev_order != b->dev_order_sent) {
+            CUDA_TRY(cudaMemcpyAsync(b->d_order, b->dev_order.data(), sizeof(int32_t) * b->dev_order.size(),
+                                     cudaMemcpyHostToDevice, c->stream));
+            CUDA_TRY(cudaStreamSynchronize(c->stream));  // the host vector may change before the copy runs
+            b->dev_order_sent = b->dev_order;
+        }
     }
     int launches = 0;
     if (c->mode == ABEA_MODE_BATCHED && c->use_graph) {
@@ -723,7 +769,7 @@ extern "C" abea_status_t abea_batch_create(abea_ctx_t* c, int32_t n_reads, const
     abea_batch* b = new (std::nothrow) abea_batch();
     if (!b) return fail(ABEA_ERR_OUT_OF_MEMORY, "host allocation failed");
     b->ctx = c;
-    if ((st = plan(b, in, (int)c->var_aware)) || (st = ensure_device(b, c->store_scores != 0)) || (st = upload(b, in, c->stream))) {
+    if ((st = plan(b, in, (int)c->var_aware, c->trace_budget)) || (st = ensure_device(b, c->store_scores != 0)) || (st = upload(b, in, c->stream))) {
         abea_batch_destroy(b);
         return st;
     }
@@ -794,12 +840,14 @@ extern "C" abea_status_t abea_batch_read_bands(abea_ctx_t* c, abea_batch_t* b, i
         return fail(ABEA_ERR_INVALID_ARG, "scores were not kept (ABEA_OPT_STORE_SCORES)");
     const ReadDesc& r = b->reads[(size_t)ri];
     if (r.skip) return ABEA_OK;
+    if (r.ck && trace) return fail(ABEA_ERR_INVALID_ARG, "read %d keeps checkpoints, not its trace (ABEA_OPT_TRACE_BUDGET)", ri);
     int64_t nb = r.n_bands, nbp = round_up(nb, 4);
     std::vector<uint8_t> tr((size_t)(nbp * kSlots));
     std::vector<int32_t> k0((size_t)nbp);
     std::vector<float> sc;
-    CUDA_TRY(cudaMemcpyAsync(tr.data(), b->d_trace + r.band_off * kSlots, tr.size(), cudaMemcpyDeviceToHost,
-                             c->stream));
+    if (!r.ck)
+        CUDA_TRY(cudaMemcpyAsync(tr.data(), b->d_trace + r.trace_off * kSlots, tr.size(), cudaMemcpyDeviceToHost,
+                                 c->stream));
     CUDA_TRY(cudaMemcpyAsync(k0.data(), b->d_band_k0 + r.band_off, sizeof(int32_t) * k0.size(),
                              cudaMemcpyDeviceToHost, c->stream));
     if (bands) {
@@ -982,7 +1030,7 @@ static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_al
         c->scratch->ctx = c;
     }
     abea_batch* b = c->scratch;
-    if ((st = plan(b, in, (int)c->var_aware)) || (st = ensure_device(b, c->store_scores != 0))) return st;
+    if ((st = plan(b, in, (int)c->var_aware, c->trace_budget)) || (st = ensure_device(b, c->store_scores != 0))) return st;
     CUDA_TRY(cudaEventRecord(c->ev[4], c->stream));
     if ((st = upload(b, in, c->stream))) return st;
     CUDA_TRY(cudaEventRecord(c->ev[5], c->stream));

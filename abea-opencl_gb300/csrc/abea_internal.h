@@ -40,7 +40,11 @@ struct ReadDesc {
     int64_t ev_src;     // first event in ev_in (reference event_ptr)
     int64_t ev_off;     // first entry in ev_mean / last_col (16-aligned)
     int64_t km_off;     // first entry in km_* (16-aligned)
-    int64_t band_off;   // first band (multiple of 4) in trace/scores/band_k0
+    int64_t band_off;   // first band (multiple of 4) in scores/band_k0
+    int64_t trace_off;  // first band (multiple of 4) of the read's trace (kept traces only)
+    int64_t ck_off;     // first float of the read's band-score checkpoints (checkpointed reads)
+    int32_t ck;         // 1: the trace is not kept; checkpoints every kCkBands bands instead
+    int32_t ck_slot;    // recompute scratch slot of a checkpointed read
     int64_t out_off;    // first pair in the output (2*event_ptr)
     int32_t n_events;
     int32_t n_kmers;    // read_len - 5
@@ -56,6 +60,14 @@ struct ReadDesc {
     int32_t skip;       // 1: nothing to align (n_kmers <= 0 or n_events <= 0)
     int32_t nonpos;     // 1: every emission of this read is <= 0 (see abea_cell.cuh)
 };
+
+// Band-score checkpoints of reads whose trace exceeds the memory budget: at
+// every band b = s*kCkBands (s >= 1) the fill stores the state it resumes from
+// (band b-1's scores, band b-2's scores shifted by one slot, band b-1's
+// placement) as one record of kCkStride floats; the traceback recomputes the
+// trace of one kCkBands-band segment at a time into a scratch slot.
+constexpr int kCkBands = 256;
+constexpr int kCkStride = 264;  // 128 + 128 scores, k0, e0, padding to 16 bytes
 
 struct GlobalConsts {
     double lp_skip;  // log(1e-10)

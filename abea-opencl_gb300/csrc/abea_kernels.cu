@@ -173,6 +173,31 @@ __device__ __forceinline__ void rings_init(Rings& rg, RingState& rs, const CoreA
     rs.e_rdy = rs.e_iss;
 }
 
+// Initial fill for a window (k0, e0) reached in the middle of a read (a resumed
+// checkpoint): the chunks that hold the window's k-mers and events, from the
+// 16-aligned chunk at or below k0 (events: e0 - 100), at most one ring's worth.
+// Caller syncs.
+__device__ __forceinline__ void rings_seek(Rings& rg, RingState& rs, const CoreArgs& a, const ReadDesc& r, int t,
+                                           int k0, int e0) {
+    rs.km_end = round_up_dev(r.n_kmers);
+    rs.ev_end = round_up_dev(r.n_events);
+    const int k_start = max(k0, 0) & ~(kChunk - 1), e_start = max(e0 - kBand, 0) & ~(kChunk - 1);
+    rs.k_iss = k_start;
+    rs.e_iss = e_start;
+    while (rs.k_iss < rs.km_end && rs.k_iss + 15 <= k0 + 127 && rs.k_iss < k_start + kSlots) {
+        issue_chunks(rg, a, r, t, true, rs.k_iss, false, 0);
+        rs.k_iss += kChunk;
+    }
+    while (rs.e_iss < rs.ev_end && rs.e_iss + 15 <= e0 + 156 && rs.e_iss < e_start + kEvRing) {
+        issue_chunks(rg, a, r, t, false, 0, true, rs.e_iss);
+        rs.e_iss += kChunk;
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    rs.k_rdy = rs.k_iss;
+    rs.e_rdy = rs.e_iss;
+}
+
 // Called once per group of bands with the current window: waits for the data the
 // next `ahead` bands need and issues the chunks whose ring entries are free.
 // Returns true when it waited (the caller then syncs the cooperating threads).
@@ -220,32 +245,87 @@ __device__ __forceinline__ uint4 transpose_bytes(uint32_t w0, uint32_t w1, uint3
                       __byte_perm(b, d, 0x7632));
 }
 
-template <bool kScores>
-__device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int lane) {
+// The bands a fill_warp call computes and where its results go.
+//   forward pass: bands [2, n_bands), band-side outputs (last column, band
+//     origins, scores, slow-cell count) written, the trace into `trace` (kept
+//     traces) or checkpoints into `ck_out` (checkpointed reads);
+//   recompute: bands [b_begin, b_end) of a checkpointed read from the record
+//     `ck_in` (nullptr: from the start), the trace into a scratch segment.
+// Trace band b is stored at trace + trace_index(b - trace_band0, slot).
+struct FillSpan {
+    int b_begin, b_end;
+    const float* ck_in;
+    float* ck_out;
+    uint8_t* trace;
+    int trace_band0;
+    bool side;
+};
+
+__device__ __forceinline__ FillSpan forward_span(const CoreArgs& a, const ReadDesc& r) {
+    FillSpan sp;
+    sp.b_begin = 2;
+    sp.b_end = r.n_bands;
+    sp.ck_in = nullptr;
+    sp.ck_out = r.ck ? a.ck + r.ck_off : nullptr;
+    sp.trace = r.ck ? nullptr : a.trace + r.trace_off * kSlots;
+    sp.trace_band0 = 0;
+    sp.side = true;
+    return sp;
+}
+
+// kSpan = false: the forward pass of a read that keeps its trace, with none of
+// the span's choices left to run time (the common case); kSpan = true: any span.
+template <bool kScores, bool kSpan>
+__device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int lane, const FillSpan& spr) {
+    FillSpan sp = spr;
+    if (!kSpan) {
+        sp.b_begin = 2;
+        sp.b_end = r.n_bands;
+        sp.ck_in = nullptr;
+        sp.ck_out = nullptr;
+        sp.trace = a.trace + r.trace_off * kSlots;
+        sp.trace_band0 = 0;
+        sp.side = true;
+    }
     const CellConsts cc = make_consts(r, a.g);
-    const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
-    uint8_t* trace = a.trace + r.band_off * kSlots;
-    float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
+    const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = sp.b_end;
+    uint8_t* trace = sp.trace;
+    float* scores = kScores && sp.side ? a.scores + r.band_off * kSlots : nullptr;
     int32_t* bk0 = a.band_k0 + r.band_off;
     float* lastc = a.last_col + r.ev_off;
 
+    // band 0: start cell (e=-1,k=-1) = 0 in slot 127; band 1: trim cell (e=0,k=-1)
+    // = (float)lp_trim, FROM_U, slot 127 (GPU/align_cuda.cl:249-268).  A resumed
+    // checkpoint gives band b_begin-1's scores and placement and band
+    // b_begin-2's scores shifted by one slot.
     int k0 = -1 - kBand / 2, e0 = kBand / 2;  // band 1 (band 0 is (49,-51), band 1 moved down)
+    float S1[4], LP[4];
+    if (kSpan && sp.ck_in) {
+        const float4 s4 = reinterpret_cast<const float4*>(sp.ck_in)[lane];
+        const float4 l4 = reinterpret_cast<const float4*>(sp.ck_in + kSlots)[lane];
+        S1[0] = s4.x; S1[1] = s4.y; S1[2] = s4.z; S1[3] = s4.w;
+        LP[0] = l4.x; LP[1] = l4.y; LP[2] = l4.z; LP[3] = l4.w;
+        k0 = __float_as_int(sp.ck_in[2 * kSlots]);
+        e0 = __float_as_int(sp.ck_in[2 * kSlots + 1]);
+    }
     RingState rs;
-    rings_init(rg, rs, a, r, lane, k0, e0);
+    if (kSpan && sp.ck_in)
+        rings_seek(rg, rs, a, r, lane, k0, e0);
+    else
+        rings_init(rg, rs, a, r, lane, k0, e0);
     __syncwarp();
 
-    // band 0: start cell (e=-1,k=-1) = 0 in slot 127; band 1: trim cell (e=0,k=-1)
-    // = (float)lp_trim, FROM_U, slot 127 (GPU/align_cuda.cl:249-268).
-    float S1[4], LP[4];
     int ep[4];  // event of each slot under the previous band's placement
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        S1[j] = LP[j] = -INFINITY;
+        if (!sp.ck_in) S1[j] = LP[j] = -INFINITY;
         ep[j] = e0 - ((4 * lane + j - k0) & 127);
     }
-    if (lane == 31) S1[3] = a.g.trim_f;
-    if (lane == 0) LP[0] = 0.0f;  // band 0 shifted by one slot = diagonal source of band 2
-    if (kScores) {
+    if (!sp.ck_in) {
+        if (lane == 31) S1[3] = a.g.trim_f;
+        if (lane == 0) LP[0] = 0.0f;  // band 0 shifted by one slot = diagonal source of band 2
+    }
+    if (kScores && scores) {
         float4 b0 = make_float4(-INFINITY, -INFINITY, -INFINITY, lane == 31 ? 0.0f : -INFINITY);
         float4 b1 = make_float4(-INFINITY, -INFINITY, -INFINITY, lane == 31 ? a.g.trim_f : -INFINITY);
         reinterpret_cast<float4*>(scores)[lane] = b0;
@@ -266,13 +346,13 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
     int my_k0 = k0;  // bands 0 and 1 (lanes 0, 1) both have k0 = -51
     unsigned long long slow = 0;
     const int sl_last = (n_kmers - 1) & 127;
-    uint32_t tw0 = 0u, tw1 = lane == 31 ? (ABEA_FROM_U << 24) : 0u, tw2 = 0u, tw3 = 0u;
+    uint32_t tw0 = 0u, tw1 = (lane == 31 && !sp.ck_in) ? (ABEA_FROM_U << 24) : 0u, tw2 = 0u, tw3 = 0u;
 
     // Band state kept across the exit to the slow path: a band in which a proof
     // failed in any lane leaves the inner loop (warp-uniform) and is finished
     // below with the reference's FP64 arithmetic, so that the inner loop holds
     // no division routine and no FP64 code.
-    int b = 2, lo = 0, hi = 0;
+    int b = sp.b_begin, lo = 0, hi = 0;
     float best[4], left[4];
     uint32_t from[4];
     bool valid[4], bad[4];
@@ -296,7 +376,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
                 best[3] = here ? tv : best[3];
                 word = here ? ((word & 0x00ffffffu) | (in ? (ABEA_FROM_U << 24) : 0u)) : word;
             }
-            if (ol >= lo && ol < hi && lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
+            if (sp.side && ol >= lo && ol < hi && lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -310,19 +390,31 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         tw2 = jb == 2 ? word : tw2;
         tw3 = jb == 3 ? word : tw3;
         if (jb == 3 || b == n_bands - 1) {
-            reinterpret_cast<uint4*>(trace + (int64_t)(b >> 2) * 512)[lane] = transpose_bytes(tw0, tw1, tw2, tw3);
+            if (!kSpan || trace)
+                reinterpret_cast<uint4*>(trace + (int64_t)((b - sp.trace_band0) >> 2) * 512)[lane] =
+                    transpose_bytes(tw0, tw1, tw2, tw3);
             tw0 = tw1 = tw2 = tw3 = 0u;
         }
-        if (kScores)
+        if (kScores && scores)
             reinterpret_cast<float4*>(scores + (int64_t)b * kSlots)[lane] = make_float4(best[0], best[1], best[2], best[3]);
         my_k0 = ((b & 31) == lane) ? k0 : my_k0;
-        if ((b & 31) == 31 || b == n_bands - 1) {
+        if (sp.side && ((b & 31) == 31 || b == n_bands - 1)) {
             if (lane <= (b & 31)) bk0[(b & ~31) + lane] = my_k0;
         }
     };
     while (true) {
         bool to_slow = false;
         for (; b < n_bands; ++b) {
+            if (kSpan && sp.ck_out && (b & (kCkBands - 1)) == 0) {
+                // checkpoint s = b / kCkBands: the state this loop resumes from at band b
+                float* rec = sp.ck_out + (int64_t)(b / kCkBands) * kCkStride;
+                reinterpret_cast<float4*>(rec)[lane] = make_float4(S1[0], S1[1], S1[2], S1[3]);
+                reinterpret_cast<float4*>(rec + kSlots)[lane] = make_float4(LP[0], LP[1], LP[2], LP[3]);
+                if (lane == 0) {
+                    rec[2 * kSlots] = __int_as_float(k0);
+                    rec[2 * kSlots + 1] = __int_as_float(e0);
+                }
+            }
             if ((b & 3) == 0) {
                 if (rings_step(rg, rs, a, r, lane, k0, e0, 6)) __syncwarp();
             }
@@ -391,7 +483,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
     }
     cp_async_wait_all();  // no copy may land in shared memory after the read is done
     __syncwarp();
-    if (slow) atomicAdd(&a.counters[0], slow);
+    if (slow && sp.side) atomicAdd(&a.counters[0], slow);
 }
 
 // ---------------------------------------------------------------- wide shape
@@ -601,7 +693,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     } else {
         // ------------------------------------------------ E0 / E1
         const int half = group - 2;
-        uint8_t* trace = a.trace + r.band_off * kSlots;
+        uint8_t* trace = a.trace + r.trace_off * kSlots;
         int32_t* bk0 = a.band_k0 + r.band_off;
         float* lastc = a.last_col + r.ev_off;
         const int sl_last = (n_kmers - 1) & 127;
@@ -680,8 +772,121 @@ __device__ double serial_path_sum(const PostArgs& a, const ReadDesc& r, const ui
     return sum;
 }
 
+// Lane 0's state of a traceback walk.
+struct Walk {
+    int k, e, n_out, gap, max_gap, last_k, last_from;
+    double sum;  // emissions of the walked cells in walk order (kSum)
+};
+
+// Walks the path from (w.k, w.e) while its band is >= band_lo.  The trace tiles
+// come from `trace` (band trace_band0 at its start; bands below bands_end exist)
+// through a shared-memory ring of four 16-band chunks (band B at ring band
+// B & 63): the chunk being walked and the one below it resident, the two below
+// those in flight.  Each walk iteration loads the bytes of the current cell and
+// of its three possible predecessors at once and takes two steps; the moves are
+// decoded arithmetically (D = 0, U = 1, L = 2: the k-mer steps back unless U,
+// the event unless L).  Cells go to out (capacity cap) or, with kSum, their
+// emissions into w.sum.  Every lane calls it; lane 0 walks.  Returns true once
+// the path has ended (k or e below 0); false when it left the segment.
+template <bool kSum>
+__device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_end, int band_lo, PostSmem& sm,
+                             int lane, Walk& w, abea_aligned_pair_t* out, int cap, const PostArgs& a,
+                             const ReadDesc& r) {
+    const int bands_pad = (bands_end + 3) & ~3;
+    const int c_lo = band_lo / kPostChunkBands;
+    auto stage = [&](int c) {  // chunk c = bands [16c, 16c + 16)
+        if (c >= c_lo) {
+            const int lo_band = c * kPostChunkBands;
+            const int bytes = min(kPostChunkBands, bands_pad - lo_band) * kSlots;
+            const uint8_t* src = trace + (int64_t)(lo_band - trace_band0) * kSlots;
+            uint8_t* dst = sm.tr + (c & 3) * (kPostChunkBands * kSlots);
+            for (int off = lane * 16; off < bytes; off += 32 * 16) cp_async16(dst + off, src + off);
+        }
+        cp_async_commit();  // an empty group keeps the group count in step
+    };
+    const uint8_t* tb = sm.tr;
+    auto T = [&](int band, int k) -> uint32_t {  // 0, 1 or 2; the clamp keeps every step a move
+        const int rb = band & 63;
+        return min((uint32_t)tb[((rb >> 2) << 9) | ((k & 127) << 2) | (rb & 3)], 2u);
+    };
+    int k = __shfl_sync(kFull, w.k, 0), e = __shfl_sync(kFull, w.e, 0);
+    int c = (e + k + 2) / kPostChunkBands;
+    stage(c);
+    stage(c - 1);
+    stage(c - 2);
+    bool ended = false, left_seg = false;
+    for (; c >= c_lo && !ended && !left_seg; --c) {
+        cp_async_wait_group1();  // chunks c and c-1 have landed; c-2 may be in flight
+        __syncwarp();
+        stage(c - 3);  // into the ring slot of chunk c+1, already walked
+        if (lane == 0) {
+            const int lo = c * kPostChunkBands;
+            auto emit = [&](int kk, int ee, uint32_t f) {
+                if (kSum)
+                    w.sum = __dadd_rn(w.sum, (double)path_emission(a, r, kk, ee));
+                else if (w.n_out < cap)
+                    out[w.n_out] = abea_aligned_pair_t{kk, ee};
+                ++w.n_out;
+                w.last_k = kk;
+                w.last_from = (int)f;
+                w.gap = (f == ABEA_FROM_L) ? w.gap + 1 : 0;
+                w.max_gap = max(w.max_gap, w.gap);
+            };
+            k = w.k;
+            e = w.e;
+            while (true) {
+                const int band = e + k + 2;
+                if ((k | e) < 0) {
+                    ended = true;
+                    break;
+                }
+                if (band < lo) {
+                    left_seg = band < band_lo;
+                    break;
+                }
+                // this cell (band >= 2) and its predecessors (bands >= lo - 2)
+                const uint32_t f0 = T(band, k), fu = T(band - 1, k);
+                const uint32_t fl = T(band - 1, k - 1), fd = T(band - 2, k - 1);
+                emit(k, e, f0);
+                const int k1 = k - (int)((f0 & 1u) ^ 1u), e1 = e - (int)((f0 >> 1) ^ 1u);
+                const uint32_t f1 = ((fd | (fu << 8) | (fl << 16)) >> (8 * f0)) & 0xffu;
+                k = k1;
+                e = e1;
+                // the second step's byte is resident unless the first left the segment
+                if ((k1 | e1) < 0 || e1 + k1 + 2 < band_lo) continue;
+                emit(k1, e1, f1);
+                k = k1 - (int)((f1 & 1u) ^ 1u);
+                e = e1 - (int)((f1 >> 1) ^ 1u);
+            }
+            w.k = k;
+            w.e = e;
+        }
+        ended = __shfl_sync(kFull, (int)ended, 0) != 0;
+        left_seg = __shfl_sync(kFull, (int)left_seg, 0) != 0;
+    }
+    cp_async_wait_all();
+    __syncwarp();
+    return ended;
+}
+
+// Recomputes the trace of segment seg (bands [seg*kCkBands, (seg+1)*kCkBands)) of
+// a checkpointed read into its scratch slot.  The whole warp calls it.
+__device__ __forceinline__ void recompute_segment(const CoreArgs& ca, const ReadDesc& r, Rings& rg, int lane, int seg) {
+    FillSpan sp;
+    sp.b_begin = max(2, seg * kCkBands);
+    sp.b_end = min((seg + 1) * kCkBands, r.n_bands);
+    sp.ck_in = seg > 0 ? ca.ck + r.ck_off + (int64_t)seg * kCkStride : nullptr;
+    sp.ck_out = nullptr;
+    sp.trace = ca.ck_scratch + (int64_t)r.ck_slot * (kCkBands * kSlots);
+    sp.trace_band0 = seg * kCkBands;
+    sp.side = false;
+    fill_warp<false, true>(ca, r, rg, lane, sp);
+    __syncwarp();
+    __threadfence_block();
+}
+
 // One warp per read: best end, traceback, QC, reverse (GPU/align_cuda.cl:618-899).
-__device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane) {
+__device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, PostSmem& sm, Rings& rg, int lane) {
     const ReadDesc r = a.reads[ri];
     if (r.skip) {
         if (lane == 0) {
@@ -719,85 +924,35 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
     if (!(best > -INFINITY)) best_e = 0;
 
     abea_aligned_pair_t* out = a.pairs + r.out_off;
-    const uint8_t* trace = a.trace + r.band_off * kSlots;
+    const uint8_t* trace = a.trace + r.trace_off * kSlots;
+    const uint8_t* ck_seg = ca.ck_scratch + (int64_t)r.ck_slot * (kCkBands * kSlots);
     const int32_t* bk0 = a.band_k0 + r.band_off;
     const int cap = r.out_cap;
     int n_out = 0, max_gap = 0, status = 0, last_k = n_kmers - 1, last_from = 0;
 
     if (best > -INFINITY) {
-        // A finite end: the path only visits computed cells.  Walked by lane 0
-        // over a shared-memory ring of four 16-band chunks of the trace (band B
-        // at ring band B & 63, the global tile layout): the chunk being walked
-        // and the one below it are resident, the two below those in flight.
-        // Each walk iteration loads the bytes of the current cell and of its
-        // three possible predecessors at once and takes two steps; the moves are
-        // decoded arithmetically (D = 0, U = 1, L = 2: the k-mer steps back
-        // unless U, the event unless L).
-        int cur_e = best_e, cur_k = n_kmers - 1, gap = 0;
-        const int bands_pad = (n_bands + 3) & ~3;
-        auto stage = [&](int c) {  // chunk c = bands [16c, 16c + 16)
-            if (c >= 0) {
-                const int lo_band = c * kPostChunkBands;
-                const int bytes = min(kPostChunkBands, bands_pad - lo_band) * kSlots;
-                const uint8_t* src = trace + (int64_t)lo_band * kSlots;
-                uint8_t* dst = sm.tr + (c & 3) * (kPostChunkBands * kSlots);
-                for (int off = lane * 16; off < bytes; off += 32 * 16) cp_async16(dst + off, src + off);
+        // A finite end: the path only visits computed cells.
+        Walk w{n_kmers - 1, best_e, 0, 0, 0, n_kmers - 1, 0, 0.0};
+        if (!r.ck) {
+            walk_segment<false>(trace, 0, n_bands, 0, sm, lane, w, out, cap, a, r);
+        } else {
+            // the trace was not kept: recompute it kCkBands bands at a time from
+            // the checkpoints, top segment first, and walk each
+            for (int seg = (w.k + w.e + 2) / kCkBands; seg >= 0; --seg) {
+                recompute_segment(ca, r, rg, lane, seg);
+                if (walk_segment<false>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands), seg * kCkBands,
+                                        sm, lane, w, out, cap, a, r))
+                    break;
             }
-            cp_async_commit();  // an empty group keeps the group count in step
-        };
-        const uint8_t* tb = sm.tr;
-        auto T = [&](int band, int k) -> uint32_t {  // 0, 1 or 2; the clamp keeps every step a move
-            const int rb = band & 63;
-            return min((uint32_t)tb[((rb >> 2) << 9) | ((k & 127) << 2) | (rb & 3)], 2u);
-        };
-        int c = (cur_e + cur_k + 2) / kPostChunkBands;
-        stage(c);
-        stage(c - 1);
-        stage(c - 2);
-        bool done = false;
-        for (; c >= 0 && !done; --c) {
-            cp_async_wait_group1();  // chunks c and c-1 have landed; c-2 may be in flight
-            __syncwarp();
-            stage(c - 3);  // into the ring slot of chunk c+1, already walked
-            if (lane == 0) {
-                const int lo = c * kPostChunkBands;
-                int k = cur_k, e = cur_e;
-                while (true) {
-                    const int band = e + k + 2;
-                    if (((k | e) < 0) || band < lo) break;
-                    // this cell (band >= 2) and its predecessors (bands >= lo - 2: resident)
-                    const uint32_t f0 = T(band, k), fu = T(band - 1, k);
-                    const uint32_t fl = T(band - 1, k - 1), fd = T(band - 2, k - 1);
-                    // step 1 from (k, e)
-                    if (n_out < cap) out[n_out] = abea_aligned_pair_t{k, e};
-                    ++n_out;
-                    last_k = k;
-                    last_from = (int)f0;
-                    gap = (f0 == ABEA_FROM_L) ? gap + 1 : 0;
-                    max_gap = max(max_gap, gap);
-                    const int k1 = k - (int)((f0 & 1u) ^ 1u), e1 = e - (int)((f0 >> 1) ^ 1u);
-                    const uint32_t f1 = ((fd | (fu << 8) | (fl << 16)) >> (8 * f0)) & 0xffu;
-                    k = k1;
-                    e = e1;
-                    if ((k1 | e1) < 0) break;
-                    // step 2 from (k1, e1): its byte was loaded with step 1's
-                    if (n_out < cap) out[n_out] = abea_aligned_pair_t{k1, e1};
-                    ++n_out;
-                    last_k = k1;
-                    last_from = (int)f1;
-                    gap = (f1 == ABEA_FROM_L) ? gap + 1 : 0;
-                    max_gap = max(max_gap, gap);
-                    k = k1 - (int)((f1 & 1u) ^ 1u);
-                    e = e1 - (int)((f1 >> 1) ^ 1u);
-                }
-                cur_k = k;
-                cur_e = e;
-                done = (k | e) < 0;
-            }
-            done = __shfl_sync(kFull, (int)done, 0) != 0;
         }
-        cp_async_wait_all();
-        __syncwarp();
+        n_out = w.n_out;
+        max_gap = w.max_gap;
+        last_k = w.last_k;
+        last_from = w.last_from;
+    } else if (lane == 0 && r.ck) {
+        // No finite end on a read whose trace was not kept: the flat-array walk
+        // below needs the whole trace.  Reported as undefined.
+        status = ABEA_ERR_UNDEFINED;
     } else if (lane == 0) {
         // No finite end: the reference walks from (0, n_kmers-1) through its flat
         // band array, where an offset outside the band reads a neighbouring row.
@@ -871,12 +1026,23 @@ __device__ void post_read_warp(const PostArgs& a, int ri, PostSmem& sm, int lane
                         sum = __dadd_rn(sum, (double)path_emission(a, r, out[i2].ref_pos, out[i2].read_pos));
                 sum = __shfl_sync(kFull, sum, 0);
             }
-        } else {
+        } else if (!r.ck) {
             sum = 0.0;
             if (lane == 0)
                 sum = serial_path_sum(a, r, trace, bk0, !(best > -INFINITY), best > -INFINITY ? best_e : 0,
                                       n_kmers - 1);
             sum = __shfl_sync(kFull, sum, 0);
+        } else {
+            // the path outgrew its output slot on a read whose trace was not kept:
+            // recompute and walk again, summing the emissions in walk order
+            Walk w{n_kmers - 1, best_e, 0, 0, 0, n_kmers - 1, 0, 0.0};
+            for (int seg = (w.k + w.e + 2) / kCkBands; seg >= 0; --seg) {
+                recompute_segment(ca, r, rg, lane, seg);
+                if (walk_segment<true>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands), seg * kCkBands,
+                                       sm, lane, w, out, cap, a, r))
+                    break;
+            }
+            sum = __shfl_sync(kFull, w.sum, 0);
         }
         const double avg = __ddiv_rn(sum, (double)n_out);
         const bool pass = !(avg < -5.0) && last_k == 0 && max_gap <= 50;
@@ -920,14 +1086,18 @@ __global__ void __launch_bounds__(32) abea_core_warp_kernel(CoreArgs a) {
     if (i >= a.n_reads) return;
     const ReadDesc& r = a.reads[i];
     if (r.skip) return;
-    fill_warp<kScores>(a, r, rg, threadIdx.x);
+    if (r.ck)
+        fill_warp<kScores, true>(a, r, rg, threadIdx.x, forward_span(a, r));
+    else
+        fill_warp<kScores, false>(a, r, rg, threadIdx.x, forward_span(a, r));
 }
 
-__global__ void __launch_bounds__(32) abea_post_kernel(PostArgs a) {
+__global__ void __launch_bounds__(32) abea_post_kernel(CoreArgs ca, PostArgs a) {
     __shared__ __align__(16) PostSmem sm;
+    __shared__ __align__(16) Rings rg;  // recompute of checkpointed reads
     const int i = blockIdx.x;
     if (i >= a.n_reads) return;
-    post_read_warp(a, i, sm, threadIdx.x);
+    post_read_warp(ca, a, i, sm, rg, threadIdx.x);
 }
 
 // ---------------------------------------------------------------- batched form
@@ -962,7 +1132,7 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         if (!r.skip) fill_wide<kScores>(a, r, sm.wide, t);
         __syncthreads();
         __threadfence_block();
-        if (warp == 0) post_read_warp(p, wide_read, sm.post[0], lane);
+        if (warp == 0) post_read_warp(a, p, wide_read, sm.post[0], sm.warp_rings[0], lane);
     }
     // phase 2: every warp pulls reads longest-first
     const int n_rest = a.n_reads - a.n_wide;
@@ -973,10 +1143,15 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         if (q >= n_rest) break;
         const int ri = a.order[a.n_wide + q];
         const ReadDesc& r = a.reads[ri];
-        if (!r.skip) fill_warp<kScores>(a, r, sm.warp_rings[warp], lane);
+        if (!r.skip) {
+            if (r.ck)
+                fill_warp<kScores, true>(a, r, sm.warp_rings[warp], lane, forward_span(a, r));
+            else
+                fill_warp<kScores, false>(a, r, sm.warp_rings[warp], lane, forward_span(a, r));
+        }
         __syncwarp();
         __threadfence_block();
-        post_read_warp(p, ri, sm.post[warp], lane);
+        post_read_warp(a, p, ri, sm.post[warp], sm.warp_rings[warp], lane);
     }
 }
 
@@ -990,7 +1165,7 @@ cudaError_t launch_plain(const LaunchArgs& la, int* launches) {
     else
         abea_core_warp_kernel<false><<<n, 32, 0, la.stream>>>(la.core);
     cudaEventRecordWithFlags(la.ev_core, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
-    abea_post_kernel<<<n, 32, 0, la.stream>>>(la.post);
+    abea_post_kernel<<<n, 32, 0, la.stream>>>(la.core, la.post);
     *launches = 3;
     return cudaGetLastError();
 }
@@ -1144,11 +1319,11 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     noalloc_write_desc<<<1, 1, 0, st>>>(d_desc, desc);
     PreArgs pre{d_desc, 1, g, sequence, events, model, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col};
     CoreArgs core{d_desc, 1, g, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col, trace, nullptr, band_k0,
-                  counters, nullptr, nullptr, 0};
+                  counters, nullptr, nullptr, 0, nullptr, nullptr};
     PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, km_rsd, last_col, trace, band_k0, pairs, n_pairs, best, status};
     abea_pre_kernel<<<1, 128, 0, st>>>(pre);
     abea_core_warp_kernel<false><<<1, 32, 0, st>>>(core);
-    abea_post_kernel<<<1, 32, 0, st>>>(post);
+    abea_post_kernel<<<1, 32, 0, st>>>(core, post);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         char msg[256];

@@ -43,6 +43,8 @@ struct CoreArgs {
     const int32_t* order;          // read indices, longest first
     int32_t* queue;                // zeroed work counters of the batched form
     int32_t n_wide;                // leading reads of `order` that run on the wide shape
+    float* ck;                     // checkpoint records of checkpointed reads
+    uint8_t* ck_scratch;           // recompute scratch: kCkBands bands of trace per checkpointed read
 };
 
 struct PostArgs {

@@ -102,8 +102,12 @@ typedef enum {
     ABEA_OPT_USE_GRAPH = 2,     /* BATCHED only: 1 = replay the three stages as one CUDA graph */
     ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide (4-warp) shape; 0 = autotuned */
     ABEA_OPT_SPIN_LIMIT = 4,    /* upper bound on any device-side wait, in polling iterations */
-    ABEA_OPT_VAR_AWARE = 5      /* 1: emissions use level_stdv*var and level_log_stdv+log_var (the
+    ABEA_OPT_VAR_AWARE = 5,     /* 1: emissions use level_stdv*var and level_log_stdv+log_var (the
                                    reference ignores var, GPU/align_cuda.cl:509); taken at batch creation */
+    ABEA_OPT_TRACE_BUDGET = 6   /* bytes of backpointers a read may keep in HBM (128 per band); a read
+                                   needing more keeps band-score checkpoints every 256 bands (4 bytes per
+                                   band) and its traceback recomputes the trace 256 bands at a time.
+                                   0 (default) = keep every trace.  Taken at batch creation. */
 } abea_option_t;
 
 typedef struct abea_ctx abea_ctx_t;
