@@ -11,13 +11,13 @@
 //  * d and u are evaluated exactly with exact_sum (below) and compared exactly;
 //    they depend only on the previous bands, so the kernels compute them before
 //    the band's exchange of neighbour cells (off the band-to-band critical path);
-//  * l is approximated in plain FP32 (error < 2^-22 relative when no term is
-//    positive, which holds for every pore model whose log_inv_sqrt_2pi -
-//    log(stdv) is <= 0); when it is below max(d, u) by more than 2^-19 of its
-//    magnitude it can neither win nor tie; otherwise it is evaluated exactly too;
+//  * l is evaluated exactly too (exact_skip), without a branch: the skip move
+//    wins in most cells away from the path (about 70% of the computed cells of
+//    the synthetic reads), so it is no rare case;
 //  * the emission's division uses a reciprocal and a proven correction step;
 //  * if any exactness proof does not go through, the cell is recomputed with
-//    native FP64 and IEEE division, literally as the reference does (cell_slow).
+//    native FP64 and IEEE division, literally as the reference does (cell_slow),
+//    outside the kernels' band loops.
 //
 // exact_sum(a, B, c) returns RN32(RN64(RN64(a + B) + c)) for floats a, c and a
 // double B = bh + bl + r (bh = RN32(B), bl = RN32(B - bh), |r| <= 2^-48|B|):
@@ -45,14 +45,12 @@ namespace abea {
 
 constexpr float kLogInvSqrt2Pi = -0.918938f;           // GPU/align_cuda.cl:66
 constexpr float kErrScale = 2.2737367544323206e-13f;   // 2^-42
-constexpr float kBelow = 1.0000019073486328f;          // 1 + 2^-19
 constexpr float kDivHi = 1.0000009536743164f;          // 1 + 2^-20
 constexpr float kDivLo = 0.99999904632568359f;         // 1 - 2^-20
 constexpr float kTiny = 7.8886090522101181e-31f;       // 2^-100
 
 struct CellConsts {
     float step_h, step_l, stay_h, stay_l, skip_h, skip_l;
-    int nonpos;      // every emission of this read is <= 0 (the skip shortcut is valid)
     double lp_step, lp_stay, lp_skip;
 };
 
@@ -232,29 +230,6 @@ __device__ __forceinline__ float pick_du(float d, float u, uint32_t& from) {
     float best = u > d ? u : d;
     from = (best == u) ? ABEA_FROM_U : ABEA_FROM_D;
     return best;
-}
-
-// Phase B: the skip (L) candidate.  When every term is <= 0 and the plain-FP32
-// approximation of l is below max(d, u) by more than 2^-19 of its magnitude
-// (its error is < 2^-22 of it), l can neither win nor tie and need not be
-// evaluated exactly.  All-(-inf) cells resolve to -inf, FROM_L (tie rule).
-// Returns need_l = true when l must be evaluated exactly (cell_l).
-__device__ __forceinline__ float cell_b(float d, float u, float left, const CellConsts& c, uint32_t& from,
-                                        bool& need_l) {
-    const float mx = u > d ? u : d;
-    const float lA = __fadd_rn(left, c.skip_h);
-    const bool below = c.nonpos && (lA < __fmul_rn(mx, kBelow));
-    const bool all_inf = (mx == -INFINITY) && (left == -INFINITY) && (d == -INFINITY);
-    need_l = !below && !all_inf;
-    float best = pick_du(d, u, from);
-    if (all_inf) from = ABEA_FROM_L;
-    return best;
-}
-
-// Exact L candidate and the reference's three-way comparison.
-__device__ __forceinline__ float cell_l(float d, float u, float left, const CellConsts& c, uint32_t& from, bool& ok) {
-    const float l = exact_sum_inf(left, c.skip_h, c.skip_l, 0.0f, ok);
-    return pick(d, u, l, from);
 }
 
 // The reference's arithmetic verbatim (IEEE division, FP64 adds): the fallback

@@ -77,7 +77,6 @@ struct abea_batch {
     abea_ctx* ctx = nullptr;
     int32_t n_reads = 0;
     int32_t var_aware = 0;       // emissions use var (ABEA_OPT_VAR_AWARE at creation)
-    float min_lsd = 0.0f;        // smallest cached log stdv of the model
     std::vector<ReadDesc> reads;
     std::vector<int32_t> order;  // longest first
     std::vector<int32_t> dev_order;       // the batched form's order: wide reads, then the rest longest first
@@ -269,11 +268,6 @@ static void split(double v, float& h, float& l) {
     l = (float)(v - (double)h);
 }
 
-static float pow2_floor(float x) {
-    int e;
-    frexpf(x, &e);  // x = m * 2^e, m in [0.5,1)
-    return ldexpf(1.0f, e - 1);
-}
 
 static GlobalConsts global_consts(int var_aware) {
     GlobalConsts g;
@@ -315,33 +309,9 @@ static abea_status_t validate(const HostInputs& in) {
 }
 
 // Offsets and per-read constants of a batch.
-// 1 when log_inv_sqrt_2pi - log(stdv) <= 0 for every k-mer of the model (with
-// the read's log_var in var-aware mode): then every emission and every score of
-// the read is <= 0, which the kernels' fast tier relies on.
-// Both roundings are monotone, so the largest K1 comes from the smallest cached
-// log stdv: the test runs on that one value per read.
-static float model_min_log_stdv(const abea_model_t* model) {
-    float m = INFINITY;
-    for (int k = 0; k < ABEA_NUM_KMER; ++k) {
-        const float v = model[k].level_log_stdv;
-        if (v != v) return v;  // NaN: no read of the batch takes the shortcut
-        if (v < m) m = v;
-    }
-    return m;
-}
-
-static int model_nonpos(float min_lsd, float log_var, int var_aware) {
-    volatile float lsd = min_lsd;
-    if (var_aware) lsd = lsd + log_var;
-    volatile float k1 = -0.918938f - lsd;
-    return k1 <= 0.0f ? 1 : 0;
-}
-
 static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, int64_t trace_budget) {
     b->n_reads = in.n_reads;
     b->var_aware = var_aware;
-    const float min_lsd = in.n_reads > 0 ? model_min_log_stdv(in.model) : 0.0f;
-    b->min_lsd = min_lsd;
     b->reads.assign((size_t)in.n_reads, ReadDesc{});
     int64_t seq_end = 0, ev_end = 0, km = 0, ev = 0, bands = 0, cells = 0, tbands = 0, ckf = 0;
     int32_t n_ck = 0;
@@ -376,9 +346,6 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, in
         r.lp_stay = p.lp_stay;
         split(p.lp_step, r.step_h, r.step_l);
         split(p.lp_stay, r.stay_h, r.stay_l);
-        r.b_max = std::max(fabsf(r.step_h), fabsf(r.stay_h));
-        r.em_floor = pow2_floor(r.b_max);
-        r.nonpos = model_nonpos(min_lsd, r.log_var, var_aware);
         r.ev_off = ev;
         r.km_off = km;
         r.band_off = bands;
@@ -665,8 +632,8 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
 }
 
 // Autotuner: times the batched form on `b` with candidate thresholds for the
-// wide (256-thread) shape — none, the heuristic, the longest eighth / quarter /
-// half of the resident blocks, and every read that fits — keeps the fastest for
+// wide shape — none, the heuristic, and the band counts of the reads ranked at
+// 1, 2, 3, 4, 6, 8, 12 and 16 sixteenths of the resident blocks — keeps the fastest for
 // this workload signature (longest read, read count and total bands, log2
 // buckets) and returns it.
 extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* best_threshold, float* best_ms) {
@@ -679,9 +646,10 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
     int64_t total = 0;
     for (const ReadDesc& r : b->reads) total += r.n_bands;
     std::vector<int64_t> cands = {INT64_MAX, std::max<int64_t>(1, total / std::max(1, blocks * 8))};
-    for (int div : {8, 4, 2, 1}) {
-        size_t k = std::min<size_t>(b->order.size(), (size_t)std::max(1, blocks / div)) - 1;
-        cands.push_back(std::max<int64_t>(1, b->reads[(size_t)b->order[k]].n_bands));
+    for (int num : {1, 2, 3, 4, 6, 8, 12, 16}) {  // the longest num/16 of the resident blocks
+        size_t k = std::min<size_t>(b->order.size(), (size_t)std::max(1, blocks * num / 16)) - 1;
+        const int64_t c = std::max<int64_t>(1, b->reads[(size_t)b->order[k]].n_bands);
+        if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
     }
     int64_t best = 0;
     float best_t = 1e30f;
@@ -922,7 +890,6 @@ static void apply_scalings(abea_batch* b, const abea_scalings_t* sc) {
         r.shift = sc[i].shift;
         r.var = sc[i].var;
         r.log_var = sc[i].log_var;
-        if (!r.skip) r.nonpos = model_nonpos(b->min_lsd, r.log_var, b->var_aware);
     }
 }
 
@@ -1165,8 +1132,7 @@ extern "C" abea_status_t abea_ctx_flush_l2(abea_ctx_t* c) {
 // ReadDesc of one read whose scratch regions all start at offset 0 (used by the
 // no-allocation entry point, which lays the regions out itself).
 namespace abea {
-ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scalings_t sc, int32_t out_capacity,
-                              int nonpos) {
+ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scalings_t sc, int32_t out_capacity) {
     ReadDesc r{};
     const int32_t nk = sequence_len - ABEA_KMER_SIZE + 1;
     r.n_events = n_events;
@@ -1184,9 +1150,6 @@ ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scali
     r.lp_stay = p.lp_stay;
     split(p.lp_step, r.step_h, r.step_l);
     split(p.lp_stay, r.stay_h, r.stay_l);
-    r.b_max = std::max(fabsf(r.step_h), fabsf(r.stay_h));
-    r.em_floor = pow2_floor(r.b_max);
-    r.nonpos = nonpos;
     return r;
 }
 GlobalConsts parity_consts() { return global_consts(0); }

@@ -55,10 +55,7 @@ struct ReadDesc {
     float step_h, step_l;  // lp_step = step_h + step_l + O(2^-48 lp_step)
     float stay_h, stay_l;
     float scale, shift, var, log_var;
-    float em_floor;     // largest power of two <= max(|step_h|, |stay_h|)
-    float b_max;        // max(|step_h|, |stay_h|)
     int32_t skip;       // 1: nothing to align (n_kmers <= 0 or n_events <= 0)
-    int32_t nonpos;     // 1: every emission of this read is <= 0 (see abea_cell.cuh)
 };
 
 // Band-score checkpoints of reads whose trace exceeds the memory budget: at

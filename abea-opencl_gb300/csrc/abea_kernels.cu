@@ -72,7 +72,6 @@ __device__ __forceinline__ CellConsts make_consts(const ReadDesc& r, const Globa
     c.stay_l = r.stay_l;
     c.skip_h = g.skip_h;
     c.skip_l = g.skip_l;
-    c.nonpos = r.nonpos;
     c.lp_step = r.lp_step;
     c.lp_stay = r.lp_stay;
     c.lp_skip = g.lp_skip;
@@ -1307,9 +1306,7 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     int32_t* status = (int32_t*)(best + 1);
     unsigned long long* counters = (unsigned long long*)carve(32);
 
-    // The pore model is not read on the host (it is device memory), so the
-    // kernels take the exact skip-candidate path for every cell (nonpos = 0).
-    const ReadDesc desc = describe_single_read(sequence_len, n_events, scaling, out_capacity, 0);
+    const ReadDesc desc = describe_single_read(sequence_len, n_events, scaling, out_capacity);
     const GlobalConsts g = parity_consts();
     // every call shares the array: clear what must start at zero
     if (cudaMemsetAsync(counters, 0, 32, st) != cudaSuccess) {

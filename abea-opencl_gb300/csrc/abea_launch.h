@@ -109,8 +109,7 @@ cudaError_t launch_batched(const LaunchArgs& a, int* launches);
 int batched_blocks_per_sm(bool scores);
 
 // Per-read constants of one read laid out at offset 0 of every scratch region.
-ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scalings_t sc, int32_t out_capacity,
-                              int nonpos);
+ReadDesc describe_single_read(int32_t sequence_len, int32_t n_events, abea_scalings_t sc, int32_t out_capacity);
 GlobalConsts parity_consts();
 
 }  // namespace abea

@@ -267,6 +267,13 @@ def adjoint_report(pkg, synth, device, seed):
     true = b.meta["true_scalings"]
     ctx = pkg.Context(device, pkg.MODE_BATCHED)
     ctx.set_option(pkg.OPT_VAR_AWARE, 1)
+    # reads over 8 kb keep band-score checkpoints every 256 bands, not their trace
+    nb8k = 8000 + int(round(8000 * 1.71)) + 2
+    budget = ((nb8k + 3) // 4) * 4 * 128
+    ctx.set_option(pkg.OPT_TRACE_BUDGET, budget)
+    nb = b.n_bands()
+    trace_bytes = ((nb + 3) // 4) * 4 * 128
+    ck = trace_bytes > budget
     dev = ctx.upload(b)
     dev.run()
     dev.sync()
@@ -297,8 +304,14 @@ def adjoint_report(pkg, synth, device, seed):
     dev.close()
     ctx.close()
     return {
-        "workload": "4096 reads U(1 kb, 10 kb); scalings perturbed by shift U(-8, 8) pA, scale x U(0.9, 1.1)",
+        "workload": "4096 reads U(1 kb, 10 kb); scalings perturbed by shift U(-8, 8) pA, scale x U(0.9, 1.1); "
+                    "reads over 8 kb checkpointed",
         "emission": "var-aware (stdv*var, log stdv + log var)",
+        "checkpointing": {"trace_budget_bytes": int(budget), "reads_checkpointed": int(ck.sum()),
+                          "every_bands": 256,
+                          "trace_bytes_kept": int(trace_bytes[~ck].sum()),
+                          "trace_bytes_replaced": int(trace_bytes[ck].sum()),
+                          "checkpoint_bytes": int(((nb[ck] // 256 + 1) * 264 * 4).sum())},
         "forward_ms": statistics.mean(fwd), "forward_band_cells_per_s": cells / (statistics.mean(fwd) / 1e3),
         "backward_ms_incl_d2h": statistics.mean(bwd), "reads_with_gradient": n_grad, "reads": b.n_reads,
         "gauss_newton": {"iterations": 3, "first_temperature": 5.0, "wall_s": t_gn,
