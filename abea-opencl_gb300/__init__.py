@@ -45,6 +45,7 @@ EXPORTS = [
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
     "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
     "abea_batch_backward", "abea_batch_set_scalings", "abea_batch_recalibrate",
+    "abea_align_db", "abea_batch_estimate_scalings",
 ]
 
 
@@ -127,6 +128,8 @@ def lib():
         L.abea_batch_backward.argtypes = [vp, vp, vp, vp, vp, vp]
         L.abea_batch_set_scalings.argtypes = [vp, vp, vp]
         L.abea_batch_recalibrate.argtypes = [vp, vp, i32, C.c_double, vp]
+        L.abea_align_db.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
+        L.abea_batch_estimate_scalings.argtypes = [vp, vp, vp, i32]
         _lib = L
     return _lib
 
@@ -208,6 +211,12 @@ class DeviceBatch:
         _check(lib().abea_batch_backward(self.ctx.h, self.h, _p(g), _p(gm), _p(em), _p(st)))
         return dict(grad_scalings=g[:n], grad_model=gm, path_emission=em[:n], status=st[:n])
 
+    def estimate_scalings(self, apply: bool = False):
+        """Method-of-moments scalings of every read (abea_batch_estimate_scalings)."""
+        out = np.zeros(max(self.batch.n_reads, 1), dtype=SCALINGS_DTYPE)
+        _check(lib().abea_batch_estimate_scalings(self.ctx.h, self.h, _p(out), 1 if apply else 0))
+        return out[: self.batch.n_reads]
+
     def set_scalings(self, scalings):
         sc = np.ascontiguousarray(scalings, dtype=SCALINGS_DTYPE)
         if len(sc) != self.batch.n_reads:
@@ -282,6 +291,28 @@ class Context:
         counts = out_counts if out_counts is not None else np.zeros(batch.n_reads, dtype=np.int32)
         _check(lib().abea_align_batch(self.h, batch.n_reads, *[_p(a) for a in arrs], _p(pairs), _p(counts)))
         return pairs, counts
+
+    def align_db(self, batch: Batch):
+        """f5c's per-read arrays (abea_align_db): one read buffer, event table and
+        output buffer per read.  Returns (list of per-read pair arrays, counts)."""
+        n = batch.n_reads
+        reads = [np.ascontiguousarray(batch.read[batch.read_ptr[i]:batch.read_ptr[i] + batch.read_len[i]])
+                 for i in range(n)]
+        evs = [np.ascontiguousarray(batch.events[batch.event_ptr[i]:batch.event_ptr[i] + batch.n_events[i]],
+                                    dtype=EVENT_DTYPE) for i in range(n)]
+        outs = [np.zeros(max(2 * int(batch.n_events[i]), 1), dtype=PAIR_DTYPE) for i in range(n)]
+        read_p = (C.c_void_p * max(n, 1))(*[r.ctypes.data for r in reads])
+        out_p = (C.c_void_p * max(n, 1))(*[o.ctypes.data for o in outs])
+        et = (_EventTable * max(n, 1))()
+        for i, e in enumerate(evs):
+            et[i].n, et[i].start, et[i].end, et[i].event = len(e), 0, len(e), e.ctypes.data
+        lens = np.ascontiguousarray(batch.read_len, dtype=np.int32)
+        sc = np.ascontiguousarray(batch.scalings, dtype=SCALINGS_DTYPE)
+        model = np.ascontiguousarray(batch.model, dtype=MODEL_DTYPE)
+        counts = np.zeros(max(n, 1), dtype=np.int32)
+        _check(lib().abea_align_db(self.h, n, read_p, _p(lens), C.cast(et, C.c_void_p), _p(sc), _p(model), out_p,
+                                   _p(counts)))
+        return [outs[i][:max(int(counts[i]), 0)] for i in range(n)], counts[:n]
 
     def last_timing(self):
         t = Timing()

@@ -128,6 +128,8 @@ struct abea_ctx {
     int64_t spin_limit = 1 << 22;
     int64_t var_aware = 0;
     int64_t trace_budget = 0;  // bytes of trace a read may keep (0 = every trace)
+    void* db_pin = nullptr;    // pinned staging of abea_align_db
+    size_t db_pin_bytes = 0;
     int sm_count = 0;
     cudaEvent_t ev[8] = {};
     cudaEvent_t marker[16] = {};
@@ -191,6 +193,7 @@ extern "C" void abea_ctx_destroy(abea_ctx_t* c) {
     for (int i = 0; i < 16; ++i)
         if (c->marker[i]) cudaEventDestroy(c->marker[i]);
     if (c->flush_buf) cudaFree(c->flush_buf);
+    if (c->db_pin) cudaFreeHost(c->db_pin);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1026,6 +1029,87 @@ extern "C" abea_status_t abea_align_batch(abea_ctx_t* c, int32_t n_reads, const 
         return fail(ABEA_ERR_INVALID_ARG, "abea_align_batch: null output");
     HostInputs in = inputs(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model);
     return align_batch_impl(c, in, event_align_pairs, n_event_align_pairs);
+}
+
+// f5c's db_t arrays: flatten into pinned staging (GPU/align_cuda.c:432-497's layout),
+// align, unflatten.
+extern "C" abea_status_t abea_align_db(abea_ctx_t* c, int32_t n_reads, char* const* read, const int32_t* read_len,
+                                       const abea_event_table_t* et, const abea_scalings_t* scalings,
+                                       const abea_model_t* model, abea_aligned_pair_t* const* pairs,
+                                       int32_t* n_pairs) {
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_align_db: null context");
+    if (n_reads < 0) return fail(ABEA_ERR_INVALID_ARG, "n_reads < 0");
+    if (n_reads == 0) return ABEA_OK;
+    if (!read || !read_len || !et || !scalings || !model || !pairs || !n_pairs)
+        return fail(ABEA_ERR_INVALID_ARG, "abea_align_db: null argument");
+    const size_t n = (size_t)n_reads;
+    std::vector<int64_t> read_ptr(n), event_ptr(n);
+    std::vector<int32_t> n_ev(n);
+    int64_t seq_bytes = 0, events = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (read_len[i] < 0 || (read_len[i] > 0 && !read[i]) || (et[i].n > 0 && !et[i].event) ||
+            et[i].n > (size_t)(1u << 30) || !pairs[i])
+            return fail(ABEA_ERR_INVALID_ARG, "abea_align_db: read %zu: bad input", i);
+        read_ptr[i] = seq_bytes;
+        seq_bytes += read_len[i] + 1;  // NUL separated
+        event_ptr[i] = events;
+        n_ev[i] = (int32_t)et[i].n;
+        events += (int64_t)et[i].n;
+    }
+    const size_t seq_sz = align256((size_t)seq_bytes), ev_sz = align256(sizeof(abea_event_t) * (size_t)events);
+    const size_t pair_sz = align256(sizeof(abea_aligned_pair_t) * (size_t)std::max<int64_t>(2 * events, 1));
+    const size_t need = seq_sz + ev_sz + pair_sz;
+    if (need > c->db_pin_bytes) {
+        if (c->db_pin) cudaFreeHost(c->db_pin);
+        c->db_pin = nullptr;
+        c->db_pin_bytes = 0;
+        CUDA_TRY(cudaSetDevice(c->device));
+        if (cudaHostAlloc(&c->db_pin, need, cudaHostAllocDefault) != cudaSuccess) {
+            c->db_pin = nullptr;
+            cudaGetLastError();
+            return fail(ABEA_ERR_OUT_OF_MEMORY, "pinned staging of %zu bytes failed", need);
+        }
+        c->db_pin_bytes = need;
+    }
+    char* seq = (char*)c->db_pin;
+    abea_event_t* ev = (abea_event_t*)(seq + seq_sz);
+    abea_aligned_pair_t* out = (abea_aligned_pair_t*)((char*)ev + ev_sz);
+    for (size_t i = 0; i < n; ++i) {
+        if (read_len[i] > 0) memcpy(seq + read_ptr[i], read[i], (size_t)read_len[i]);
+        seq[read_ptr[i] + read_len[i]] = 0;
+        if (et[i].n > 0) memcpy(ev + event_ptr[i], et[i].event, sizeof(abea_event_t) * et[i].n);
+    }
+    HostInputs in = inputs(n_reads, seq, read_ptr.data(), read_len, ev, event_ptr.data(), n_ev.data(), scalings, model);
+    const abea_status_t st = align_batch_impl(c, in, out, n_pairs);
+    // per-read statuses (capacity, undefined) leave the other reads' results valid
+    if (st != ABEA_OK && st != ABEA_ERR_CAPACITY && st != ABEA_ERR_UNDEFINED) return st;
+    for (size_t i = 0; i < n; ++i)
+        if (n_pairs[i] > 0) memcpy(pairs[i], out + 2 * event_ptr[i], sizeof(abea_aligned_pair_t) * (size_t)n_pairs[i]);
+    return st;
+}
+
+// Method-of-moments scalings of a device-resident batch.
+extern "C" abea_status_t abea_batch_estimate_scalings(abea_ctx_t* c, abea_batch_t* b, abea_scalings_t* out,
+                                                      int32_t apply) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_estimate_scalings: null argument");
+    if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
+    if (b->n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    const size_t n = (size_t)b->n_reads;
+    MomArgs m{b->d_reads, b->n_reads, b->d_seq, b->d_ev, b->d_model, b->d_gn};  // d_gn: [n][5] scratch
+    cudaError_t e = launch_mom(m, c->stream);
+    if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "moment kernel launch failed: %s", cudaGetErrorString(e));
+    std::vector<double> v(2 * n);
+    CUDA_TRY(cudaMemcpyAsync(v.data(), b->d_gn, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    std::vector<abea_scalings_t> sc(n);
+    for (size_t i = 0; i < n; ++i) sc[i] = abea_scalings_t{(float)v[2 * i], (float)v[2 * i + 1], 1.0f, 0.0f};
+    if (out) memcpy(out, sc.data(), sizeof(abea_scalings_t) * n);
+    if (apply) {
+        apply_scalings(b, sc.data());
+        return upload_reads(c, b);
+    }
+    return ABEA_OK;
 }
 
 extern "C" abea_status_t abea_ctx_last_timing(abea_ctx_t* c, abea_timing_t* t, int64_t* h2d, int64_t* d2h) {

@@ -1415,3 +1415,57 @@ cudaError_t launch_adjoint(const AdjArgs& a, cudaStream_t stream) {
 }
 
 }  // namespace abea
+
+// ---------------------------------------------------------------- method of moments
+// f5c's estimate_scalings_using_mom (GPU/f5cmisc.h:47; its body is not part of the
+// reference): the scale and shift that map the k-mer levels along the read onto
+// the event means' mean and variance.  FP64 sums, one warp per read.
+namespace abea {
+
+__global__ void __launch_bounds__(32) abea_mom_kernel(MomArgs a) {
+    const int ri = blockIdx.x, lane = threadIdx.x;
+    if (ri >= a.n_reads) return;
+    const ReadDesc r = a.reads[ri];
+    double es = 0.0, es2 = 0.0, ks = 0.0, ks2 = 0.0;
+    if (!r.skip) {
+        for (int e = lane; e < r.n_events; e += 32) {
+            const double x = a.ev[r.ev_src + e].mean;
+            es += x;
+            es2 += x * x;
+        }
+        const char* s = a.seq + r.seq_off;
+        for (int k = lane; k < r.n_kmers; k += 32) {
+            uint32_t rank = 0;
+#pragma unroll
+            for (int q = 0; q < ABEA_KMER_SIZE; ++q) rank = (rank << 2) | base_rank(s[k + q]);
+            const double l = a.model[rank].level_mean;
+            ks += l;
+            ks2 += l * l;
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        es += __shfl_xor_sync(kFull, es, off);
+        es2 += __shfl_xor_sync(kFull, es2, off);
+        ks += __shfl_xor_sync(kFull, ks, off);
+        ks2 += __shfl_xor_sync(kFull, ks2, off);
+    }
+    if (lane == 0) {
+        double scale = 1.0, shift = 0.0;
+        if (!r.skip) {
+            const double em = es / r.n_events, ev = es2 / r.n_events - em * em;
+            const double km = ks / r.n_kmers, kv = ks2 / r.n_kmers - km * km;
+            scale = sqrt(ev / kv);
+            shift = em - scale * km;
+        }
+        a.out[2 * ri] = scale;
+        a.out[2 * ri + 1] = shift;
+    }
+}
+
+cudaError_t launch_mom(const MomArgs& a, cudaStream_t stream) {
+    if (a.n_reads > 0) abea_mom_kernel<<<a.n_reads, 32, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace abea

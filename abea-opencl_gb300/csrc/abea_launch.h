@@ -90,6 +90,18 @@ struct AdjArgs {
 // Backward pass over the stored paths of a finished forward run.
 cudaError_t launch_adjoint(const AdjArgs& a, cudaStream_t stream);
 
+struct MomArgs {
+    const ReadDesc* reads;
+    int n_reads;
+    const char* seq;
+    const abea_event_t* ev;
+    const abea_model_t* model;
+    double* out;  // [n][2]: scale, shift
+};
+
+// Method-of-moments scalings, one warp per read.
+cudaError_t launch_mom(const MomArgs& a, cudaStream_t stream);
+
 struct LaunchArgs {
     PreArgs pre;
     CoreArgs core;

@@ -169,6 +169,16 @@ abea_status_t abea_align_batch(abea_ctx_t *ctx, int32_t n_reads, const char *rea
                                const abea_model_t *model, abea_aligned_pair_t *event_align_pairs,
                                int32_t *n_event_align_pairs);
 
+/* f5c's per-read arrays (db_t's read[i], read_len[i], et[i], scalings[i],
+ * event_align_pairs[i], n_event_align_pairs[i]; GPU/f5c.h) aligned as one batch:
+ * the flattening of GPU/align_cuda.c:432-497 done inside the library, through
+ * pinned staging kept by the context.  event_align_pairs[i] must hold
+ * 2*et[i].n pairs; n_event_align_pairs[i] as in abea_align_batch. */
+abea_status_t abea_align_db(abea_ctx_t *ctx, int32_t n_reads, char *const *read, const int32_t *read_len,
+                            const abea_event_table_t *et, const abea_scalings_t *scalings,
+                            const abea_model_t *model, abea_aligned_pair_t *const *event_align_pairs,
+                            int32_t *n_event_align_pairs);
+
 /* ---- device-resident batches --------------------------------------------
  * abea_batch_create copies a batch (same host layout as abea_align_batch) into
  * HBM once; abea_batch_run aligns it on the context's stream (asynchronous);
@@ -272,6 +282,15 @@ abea_status_t abea_batch_set_scalings(abea_ctx_t *ctx, abea_batch_t *batch, cons
  * (may be NULL). */
 abea_status_t abea_batch_recalibrate(abea_ctx_t *ctx, abea_batch_t *batch, int32_t iterations,
                                      double first_temperature, abea_scalings_t *out);
+
+/* Method-of-moments scalings of every read of a batch (f5c's
+ * estimate_scalings_using_mom, GPU/f5cmisc.h:47, prototype only in the
+ * reference): scale = sqrt(var(event means) / var(k-mer levels along the read)),
+ * shift = mean(event means) - scale * mean(k-mer levels), var = 1, log_var = 0,
+ * sums in FP64.  Written to out[n_reads] (may be NULL); apply != 0 also makes
+ * them the batch's scalings for the next run. */
+abea_status_t abea_batch_estimate_scalings(abea_ctx_t *ctx, abea_batch_t *batch, abea_scalings_t *out,
+                                           int32_t apply);
 
 /* ---- no-allocation entry point ------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

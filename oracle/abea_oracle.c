@@ -565,3 +565,33 @@ double oracle_path_adjoint(const abea_aligned_pair_t *walk, int32_t n, int32_t l
         for (int i = 0; i < 5; ++i) gn5[i] = h[i];
     return em_sum;
 }
+
+/* ---- method-of-moments scalings (no counterpart in the reference) ----
+ * f5c's estimate_scalings_using_mom is only a prototype in the reference
+ * (GPU/f5cmisc.h:47); restated from the method of moments: the scale and shift
+ * that map the k-mer levels along the read onto the mean and variance of the
+ * event means.  FP64 serial sums. */
+void oracle_mom(const char *seq, int32_t seq_len, const abea_event_t *events, int32_t n_events,
+                const abea_model_t *model, double *scale, double *shift) {
+    const int32_t n_kmers = seq_len - ABEA_KMER_SIZE + 1;
+    if (n_kmers <= 0 || n_events <= 0) {
+        *scale = 1.0;
+        *shift = 0.0;
+        return;
+    }
+    double es = 0, es2 = 0, ks = 0, ks2 = 0;
+    for (int32_t e = 0; e < n_events; ++e) {
+        const double x = events[e].mean;
+        es += x;
+        es2 += x * x;
+    }
+    for (int32_t k = 0; k < n_kmers; ++k) {
+        const double l = model[oracle_kmer_rank(seq + k)].level_mean;
+        ks += l;
+        ks2 += l * l;
+    }
+    const double em = es / n_events, ev = es2 / n_events - em * em;
+    const double km = ks / n_kmers, kv = ks2 / n_kmers - km * km;
+    *scale = sqrt(ev / kv);
+    *shift = em - *scale * km;
+}

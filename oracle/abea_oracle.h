@@ -90,6 +90,13 @@ double oracle_path_adjoint(const abea_aligned_pair_t *walk, int32_t n, int32_t l
                            double d_stdv, uint32_t flags, double *grad3, double *gn5,
                            double *grad_model);
 
+/* Method-of-moments scalings of one read (f5c's estimate_scalings_using_mom,
+ * prototype only in the reference, GPU/f5cmisc.h:47): scale = sqrt(var(event
+ * means) / var(k-mer levels along the read)), shift = mean(event means) -
+ * scale * mean(k-mer levels); FP64; (1, 0) for a read with nothing to align. */
+void oracle_mom(const char *seq, int32_t seq_len, const abea_event_t *events, int32_t n_events,
+                const abea_model_t *model, double *scale, double *shift);
+
 /* Rank of the 6-mer starting at s (GPU/align_cuda.cl:22-51). */
 uint32_t oracle_kmer_rank(const char *s);
 

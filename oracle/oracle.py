@@ -71,6 +71,9 @@ def lib():
         L.oracle_path_adjoint.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_char_p, C.c_void_p,
                                           C.c_void_p, _Scalings, C.c_void_p, C.c_int32, C.c_double,
                                           C.c_double, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_mom.restype = None
+        L.oracle_mom.argtypes = [C.c_char_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.oracle_n_bands.restype = C.c_int64
         L.oracle_n_bands.argtypes = [C.c_int32, C.c_int32]
         _lib = L
@@ -167,6 +170,15 @@ def path_adjoint(walk, last_from: int, seq: bytes, events, model, scalings, flag
                                    _ptr(model), _sc(scalings), _ptr(th), int(kmer), float(d_mean),
                                    float(d_stdv), flags, _ptr(g), _ptr(gn), _ptr(gm))
     return em, g, gn, gm
+
+
+def mom(seq: bytes, events, model):
+    """Method-of-moments (scale, shift) of one read, FP64."""
+    events = np.ascontiguousarray(events, dtype=EVENT_DTYPE)
+    model = np.ascontiguousarray(model, dtype=MODEL_DTYPE)
+    sc, sh = C.c_double(), C.c_double()
+    lib().oracle_mom(bytes(seq), len(seq), _ptr(events), len(events), _ptr(model), C.byref(sc), C.byref(sh))
+    return sc.value, sh.value
 
 
 def add3(a: float, b: float, c: float) -> float:

@@ -1,0 +1,79 @@
+"""f5c-facing entries beyond align(): the per-read-array batch call (f5c's db_t,
+`abea_align_db`) and the method-of-moments scalings (f5c's
+estimate_scalings_using_mom, `abea_batch_estimate_scalings`)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, abea
+
+
+def read_of(batch, i):
+    seq = bytes(batch.read[batch.read_ptr[i]:batch.read_ptr[i] + batch.read_len[i]])
+    ev = batch.events[batch.event_ptr[i]:batch.event_ptr[i] + batch.n_events[i]]
+    return seq, ev
+
+
+def test_header_compiles_as_c_and_links(tmp_path):
+    """A C caller of the f5c-style entries builds against include/abea.h and the library."""
+    if not os.path.exists(abea.LIB_PATH):
+        abea.build()
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "abea.h"\n'
+        "int use(abea_ctx_t *ctx, int n, char *const *read, const int *len, const abea_event_table_t *et,\n"
+        "        const abea_scalings_t *sc, const abea_model_t *m, abea_aligned_pair_t *const *out, int *cnt) {\n"
+        "    return (int)abea_align_db(ctx, n, read, len, et, sc, m, out, cnt);\n"
+        "}\n"
+        "int main(void) { return use(0, 0, 0, 0, 0, 0, 0, 0, 0) == ABEA_ERR_INVALID_ARG ? 0 : 1; }\n")
+    lib_dir = os.path.dirname(abea.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-L", lib_dir, "-labea", "-o", str(tmp_path / "caller")], check=True)
+
+
+def test_oracle_mom_is_close_to_the_generating_scalings(oracle_mod):
+    from abea_gb300 import synth
+    b = synth.make_batch("adjoint", seed=13, lengths=[3000, 5000, 8000])
+    true = b.meta["true_scalings"]
+    for i in range(b.n_reads):
+        seq, ev = read_of(b, i)
+        scale, shift = oracle_mod.mom(seq, ev, b.model)
+        # event counts per k-mer and skipped k-mers weight the moments a little
+        assert abs(scale / true["scale"][i] - 1) < 0.05
+        assert abs(shift - true["shift"][i]) < 5.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [abea.MODE_PLAIN, abea.MODE_BATCHED])
+def test_align_db_equals_align_batch(mode, ref_synthetic):
+    from abea_gb300 import synth
+    for batch in (synth.make_batch("small", seed=6), ref_synthetic[0]):
+        ctx = abea.Context(0, mode)
+        pairs, counts = ctx.align_batch(batch)
+        per_read, c2 = ctx.align_db(batch)
+        assert np.array_equal(counts, c2)
+        for x, y in zip(abea.split_pairs(batch, pairs, counts), per_read):
+            assert np.array_equal(x, y)
+
+
+@pytest.mark.gpu
+def test_gpu_mom_matches_the_oracle_and_seeds_recalibration(oracle_mod):
+    from abea_gb300 import synth
+    rng = np.random.default_rng(8)
+    batch = synth.make_batch("adjoint", seed=17, lengths=rng.integers(1000, 10001, 64))
+    true = batch.meta["true_scalings"]
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    dev = ctx.upload(batch)
+    sc = dev.estimate_scalings(apply=True)
+    for i in range(batch.n_reads):
+        seq, ev = read_of(batch, i)
+        scale, shift = oracle_mod.mom(seq, ev, batch.model)
+        assert abs(sc["scale"][i] - scale) <= 1e-6 * abs(scale)
+        assert abs(sc["shift"][i] - shift) <= 1e-5 * max(abs(shift), 1.0)
+    assert np.all(sc["var"] == 1.0) and np.all(sc["log_var"] == 0.0)
+    # method of moments, then annealed Gauss-Newton: f5c's scale -> align -> recalibrate loop
+    fit = dev.recalibrate(3, first_temperature=5.0)
+    ok = (np.abs(fit["shift"] - true["shift"]) < 1.0) & (np.abs(fit["scale"] / true["scale"] - 1) < 0.01)
+    assert ok.mean() >= 0.9, ok.mean()
