@@ -203,6 +203,7 @@ __device__ __forceinline__ void rings_seek(Rings& rg, RingState& rs, const CoreA
 __device__ __forceinline__ bool rings_step(Rings& rg, RingState& rs, const CoreArgs& a, const ReadDesc& r, int t,
                                            int k0, int e0, int ahead) {
     bool waited = false;
+    const int k_prev = rs.k_iss, e_prev = rs.e_iss;  // issued before this call
     const bool do_k = rs.k_iss < rs.km_end && rs.k_iss + 15 <= k0 + 127;
     const bool do_e = rs.e_iss < rs.ev_end && rs.e_iss + 15 <= e0 + 156;
     if (do_k || do_e) {
@@ -211,10 +212,20 @@ __device__ __forceinline__ bool rings_step(Rings& rg, RingState& rs, const CoreA
         if (do_k) rs.k_iss += kChunk;
         if (do_e) rs.e_iss += kChunk;
     }
-    if ((k0 + kBand - 1 + ahead >= rs.k_rdy && rs.k_rdy < rs.km_end) || (e0 + ahead >= rs.e_rdy && rs.e_rdy < rs.ev_end)) {
-        cp_async_wait_all();
-        rs.k_rdy = rs.k_iss;
-        rs.e_rdy = rs.e_iss;
+    auto needs = [&](int k_have, int e_have) {
+        return (k0 + kBand - 1 + ahead >= k_have && k_have < rs.km_end) || (e0 + ahead >= e_have && e_have < rs.ev_end);
+    };
+    if (needs(rs.k_rdy, rs.e_rdy)) {
+        if ((do_k || do_e) && !needs(k_prev, e_prev)) {
+            // the chunks just issued are not needed yet: wait for the older ones only
+            cp_async_wait_group1();
+            rs.k_rdy = k_prev;
+            rs.e_rdy = e_prev;
+        } else {
+            cp_async_wait_all();
+            rs.k_rdy = rs.k_iss;
+            rs.e_rdy = rs.e_iss;
+        }
         waited = true;
     }
     return waited;
