@@ -17,6 +17,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import weakref
 
 import numpy as np
 
@@ -45,7 +46,7 @@ EXPORTS = [
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
     "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
     "abea_batch_backward", "abea_batch_set_scalings", "abea_batch_recalibrate",
-    "abea_align_db", "abea_batch_estimate_scalings",
+    "abea_align_db", "abea_batch_estimate_scalings", "abea_align_stream",
 ]
 
 
@@ -67,6 +68,18 @@ class Timing(C.Structure):
     _fields_ = [("pre_ms", C.c_float), ("core_ms", C.c_float), ("post_ms", C.c_float),
                 ("total_ms", C.c_float), ("h2d_ms", C.c_float), ("d2h_ms", C.c_float),
                 ("kernel_launches", C.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class StreamConfig(C.Structure):
+    _fields_ = [("batch_bytes", C.c_int64), ("recalibrate", C.c_int32), ("reserved", C.c_int32)]
+
+
+class StreamStats(C.Structure):
+    _fields_ = [("n_batches", C.c_int32), ("max_batch_reads", C.c_int32), ("max_batch_bytes", C.c_int64),
+                ("band_cells", C.c_int64), ("wall_ms", C.c_double), ("compute_ms", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -130,8 +143,35 @@ def lib():
         L.abea_batch_recalibrate.argtypes = [vp, vp, i32, C.c_double, vp]
         L.abea_align_db.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
         L.abea_batch_estimate_scalings.argtypes = [vp, vp, vp, i32]
+        L.abea_align_stream.argtypes = [vp, C.POINTER(StreamConfig), i32] + [vp] * 13
         _lib = L
     return _lib
+
+
+def pinned_empty(n: int, dtype) -> np.ndarray:
+    """A 1-D array of `n` elements in pinned host memory (abea_host_alloc), freed
+    when the array is collected: copies from and to it overlap device work."""
+    dt = np.dtype(dtype)
+    nbytes = max(int(n) * dt.itemsize, 1)
+    p = lib().abea_host_alloc(nbytes)
+    if not p:
+        raise AbeaError(-3, f"pinned host allocation of {nbytes} bytes failed")
+    buf = (C.c_char * nbytes).from_address(p)
+    weakref.finalize(buf, lib().abea_host_free, p)
+    return np.frombuffer(buf, dtype=dt, count=int(n))
+
+
+def pin_batch(b: Batch) -> Batch:
+    """The batch with every array copied into pinned host memory."""
+    def pin(a, dtype):
+        a = np.asarray(a, dtype=dtype)
+        out = pinned_empty(a.size, dtype)
+        out[:] = a.reshape(-1)
+        return out
+    return Batch(read=pin(b.read, np.uint8), read_ptr=pin(b.read_ptr, np.int64), read_len=pin(b.read_len, np.int32),
+                 events=pin(b.events, EVENT_DTYPE), event_ptr=pin(b.event_ptr, np.int64),
+                 n_events=pin(b.n_events, np.int32), scalings=pin(b.scalings, SCALINGS_DTYPE),
+                 model=pin(b.model, MODEL_DTYPE), meta=dict(b.meta))
 
 
 def _check(st: int):
@@ -314,6 +354,27 @@ class Context:
                                    _p(counts)))
         return [outs[i][:max(int(counts[i]), 0)] for i in range(n)], counts[:n]
 
+    def align_stream(self, batch: Batch, batch_bytes: int = 0, recalibrate: bool = False, out_pairs=None,
+                     out_counts=None):
+        """The batch as a serving stream (abea_align_stream): admitted in order into
+        device batches of at most `batch_bytes` (0 = library default), two in
+        flight; with `recalibrate`, each device batch is aligned, differentiated,
+        given one Gauss-Newton step of (shift, scale) and re-aligned.  Returns a
+        dict: pairs, counts, scalings (final per read), latency_ms (per read, from
+        its batch's admission to its results on the host) and stats."""
+        arrs = _batch_arrays(batch)
+        n = batch.n_reads
+        pairs = out_pairs if out_pairs is not None else np.zeros(max(batch.pair_capacity(), 1), dtype=PAIR_DTYPE)
+        counts = out_counts if out_counts is not None else np.zeros(max(n, 1), dtype=np.int32)
+        sc_out = np.zeros(max(n, 1), dtype=SCALINGS_DTYPE)
+        lat = np.zeros(max(n, 1), dtype=np.float64)
+        cfg = StreamConfig(int(batch_bytes), 1 if recalibrate else 0, 0)
+        stats = StreamStats()
+        _check(lib().abea_align_stream(self.h, C.byref(cfg), n, *[_p(a) for a in arrs], _p(pairs), _p(counts),
+                                       _p(sc_out), _p(lat), C.byref(stats)))
+        return {"pairs": pairs, "counts": counts[:n], "scalings": sc_out[:n], "latency_ms": lat[:n],
+                "stats": stats.as_dict()}
+
     def last_timing(self):
         t = Timing()
         h2d, d2h = C.c_int64(), C.c_int64()
@@ -369,4 +430,4 @@ def version() -> str:
 
 __all__ = ["align", "Context", "DeviceBatch", "Batch", "from_reads", "split_pairs", "build", "lib",
            "AbeaError", "MODE_PLAIN", "MODE_BATCHED", "types", "EXPORTS", "version",
-           "selftest_arith"]
+           "selftest_arith", "pinned_empty", "pin_batch", "StreamConfig", "StreamStats"]

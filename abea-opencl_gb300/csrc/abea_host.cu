@@ -12,6 +12,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <map>
 #include <mutex>
 #include <new>
@@ -115,7 +116,8 @@ struct abea_batch {
     bool ran = false;
     abea_timing_t timing{};
     cudaGraphExec_t graph = nullptr;  // batched form: memsets + pre + fused core/post
-    uint64_t graph_key[4] = {0, 0, 0, 0};
+    std::vector<uint64_t> carve;      // slab base and region sizes: every device pointer follows from them
+    std::vector<uint64_t> graph_key;  // what the captured graph's launch arguments were built from
 };
 
 struct abea_ctx {
@@ -136,6 +138,10 @@ struct abea_ctx {
     void* flush_buf = nullptr;
     size_t flush_bytes = 0;
     abea_batch* scratch = nullptr;  // reused by abea_align_batch / abea_align
+    // serving stream: two device batches, their copy stream and events (created on first use)
+    abea_batch* sslot[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t sev[2][4] = {};  // per slot: uploaded, compute start, compute end, results copied
     std::map<uint64_t, int64_t> tuned;  // autotuned wide-shape threshold per workload signature
 };
 
@@ -188,6 +194,12 @@ extern "C" void abea_ctx_destroy(abea_ctx_t* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->scratch) abea_batch_destroy(c->scratch);
+    for (int i = 0; i < 2; ++i) {
+        if (c->sslot[i]) abea_batch_destroy(c->sslot[i]);
+        for (int j = 0; j < 4; ++j)
+            if (c->sev[i][j]) cudaEventDestroy(c->sev[i][j]);
+    }
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (int i = 0; i < 8; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 16; ++i)
@@ -390,7 +402,7 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, in
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Carves the device slab; grows it when needed.
-static abea_status_t ensure_device(abea_batch* b, bool scores) {
+static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 0) {
     size_t n = (size_t)std::max(b->n_reads, 1);
     size_t sizes[31] = {
         sizeof(ReadDesc) * n,                                   // reads
@@ -430,14 +442,15 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
     if (total > b->slab.bytes) {
         free_batch_device(b);
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, total);
+        const size_t want = std::max(total, reserve);
+        cudaError_t e = cudaMalloc(&p, want);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return fail(ABEA_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed: %s", total,
+            return fail(ABEA_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed: %s", want,
                         cudaGetErrorString(e));
         }
         b->slab.base = p;
-        b->slab.bytes = total;
+        b->slab.bytes = want;
     }
     char* p = (char*)b->slab.base;
     void* ptrs[31];
@@ -476,6 +489,8 @@ static abea_status_t ensure_device(abea_batch* b, bool scores) {
     b->d_ck = (float*)ptrs[28];
     b->d_ck_scratch = (uint8_t*)ptrs[29];
     b->scores_kept = scores;
+    b->carve.assign(1, (uint64_t)(uintptr_t)b->slab.base);
+    for (int i = 0; i < n_bufs; ++i) b->carve.push_back((uint64_t)sizes[i]);
     return ABEA_OK;
 }
 
@@ -571,6 +586,19 @@ static abea_status_t queue_work(abea_ctx* c, abea_batch* b, int* launches, bool 
     return launch_all(c, b, launches, capturing);
 }
 
+// The batched form's order: wide reads (threshold from the option, else the
+// autotuned value of this workload signature, else the heuristic) then the rest.
+static void prepare_order(abea_ctx* c, abea_batch* b) {
+    b->n_wide = 0;
+    if (c->mode != ABEA_MODE_BATCHED) return;
+    int64_t thr = c->long_read_bands;
+    if (thr == 0) {
+        auto it = c->tuned.find(workload_signature(b));
+        if (it != c->tuned.end()) thr = it->second;
+    }
+    b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept);
+}
+
 static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
     CUDA_TRY(cudaSetDevice(c->device));
     b->timing = abea_timing_t{};
@@ -579,14 +607,8 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
         return ABEA_OK;
     }
     // wide shape for the longest reads in the batched form
-    b->n_wide = 0;
+    prepare_order(c, b);
     if (c->mode == ABEA_MODE_BATCHED) {
-        int64_t thr = c->long_read_bands;
-        if (thr == 0) {
-            auto it = c->tuned.find(workload_signature(b));
-            if (it != c->tuned.end()) thr = it->second;
-        }
-        b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept);
         if (b->dev_order != b->dev_order_sent) {
             CUDA_TRY(cudaMemcpyAsync(b->d_order, b->dev_order.data(), sizeof(int32_t) * b->dev_order.size(),
                                      cudaMemcpyHostToDevice, c->stream));
@@ -597,9 +619,13 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
     int launches = 0;
     if (c->mode == ABEA_MODE_BATCHED && c->use_graph) {
         // the whole run as one CUDA graph, re-captured when its parameters change
-        const uint64_t key[4] = {(uint64_t)(uintptr_t)b->slab.base, (uint64_t)b->n_reads, (uint64_t)b->n_wide,
-                                 (uint64_t)(b->scores_kept ? 1 : 0) | ((uint64_t)b->var_aware << 1)};
-        if (!b->graph || memcmp(key, b->graph_key, sizeof(key)) != 0) {
+        // the kernels' arguments (device pointers, counts, constants) follow from
+        // the slab layout and these; any change re-captures
+        std::vector<uint64_t> key = b->carve;
+        key.push_back((uint64_t)b->n_reads);
+        key.push_back((uint64_t)b->n_wide);
+        key.push_back((uint64_t)(b->scores_kept ? 1 : 0) | ((uint64_t)b->var_aware << 1));
+        if (!b->graph || key != b->graph_key) {
             if (b->graph) cudaGraphExecDestroy(b->graph);
             b->graph = nullptr;
             cudaGraph_t g = nullptr;
@@ -617,7 +643,7 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
                 b->graph = nullptr;
                 return fail(ABEA_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
             }
-            memcpy(b->graph_key, key, sizeof(key));
+            b->graph_key = key;
         }
         launches = 2;
         CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
@@ -912,6 +938,24 @@ extern "C" abea_status_t abea_batch_set_scalings(abea_ctx_t* c, abea_batch_t* b,
     return upload_reads(c, b);
 }
 
+// One Gauss-Newton step of every read's (shift, scale) from the fixed-path
+// normal equations gn[5*i] = {h00, h01, h11, t0, t1} of the adjoint kernel.
+static void gn_step(const abea_batch* b, const double* gn, const int32_t* ast, abea_scalings_t* sc) {
+    for (size_t i = 0; i < (size_t)b->n_reads; ++i) {
+        if (ast[i] != 0 || b->reads[i].skip) continue;
+        const double* h = &gn[5 * i];
+        const double det = h[0] * h[2] - h[1] * h[1];
+        if (!(det > 1e-12 * h[0] * h[2])) continue;  // fewer than two distinct levels on the path
+        // [h0 h1; h1 h2] (d_shift, d_scale) = -(t1, t2)
+        const double ds = (-h[3] * h[2] + h[4] * h[1]) / det;
+        const double dk = (-h[4] * h[0] + h[3] * h[1]) / det;
+        const double ns = (double)sc[i].shift + ds, nk = (double)sc[i].scale + dk;
+        if (!std::isfinite(ns) || !std::isfinite(nk) || !(nk > 0.0)) continue;
+        sc[i].shift = (float)ns;
+        sc[i].scale = (float)nk;
+    }
+}
+
 // Gauss-Newton on (shift, scale): the residuals (x - scale*mu - shift)/sd of the
 // emitting cells of the fixed path are linear in (shift, scale), so one step
 // solves the weighted least-squares problem on that path exactly; re-aligning
@@ -961,19 +1005,7 @@ extern "C" abea_status_t abea_batch_recalibrate(abea_ctx_t* c, abea_batch_t* b, 
             st = fail(ABEA_ERR_CUDA, "recalibration: %s", cudaGetErrorString(e));
             break;
         }
-        for (size_t i = 0; i < n; ++i) {
-            if (ast[i] != 0 || b->reads[i].skip) continue;
-            const double* h = &gn[5 * i];
-            const double det = h[0] * h[2] - h[1] * h[1];
-            if (!(det > 1e-12 * h[0] * h[2])) continue;  // fewer than two distinct levels on the path
-            // [h0 h1; h1 h2] (d_shift, d_scale) = -(t1, t2)
-            const double ds = (-h[3] * h[2] + h[4] * h[1]) / det;
-            const double dk = (-h[4] * h[0] + h[3] * h[1]) / det;
-            const double ns = (double)sc[i].shift + ds, nk = (double)sc[i].scale + dk;
-            if (!std::isfinite(ns) || !std::isfinite(nk) || !(nk > 0.0)) continue;
-            sc[i].shift = (float)ns;
-            sc[i].scale = (float)nk;
-        }
+        gn_step(b, gn.data(), ast.data(), sc.data());
     }
     // the batch keeps its own emission mode and the final scalings
     b->var_aware = va0;
@@ -1108,6 +1140,258 @@ extern "C" abea_status_t abea_batch_estimate_scalings(abea_ctx_t* c, abea_batch_
     if (apply) {
         apply_scalings(b, sc.data());
         return upload_reads(c, b);
+    }
+    return ABEA_OK;
+}
+
+// ---------------------------------------------------------------- serving stream
+// Device bytes one read adds to a batch's slab (the per-read terms of
+// ensure_device), and the slab's fixed part (model, model gradient, counters,
+// alignment padding).
+static int64_t read_device_bytes(int32_t len, int32_t ne, int64_t trace_budget, bool scores) {
+    const int64_t nk = (int64_t)len - ABEA_KMER_SIZE + 1;
+    int64_t bytes = (int64_t)sizeof(ReadDesc) + len + 1 + (int64_t)sizeof(abea_event_t) * ne +
+                    (int64_t)sizeof(abea_aligned_pair_t) * 2 * ne +
+                    8 * (int64_t)sizeof(int32_t) + 9 * (int64_t)sizeof(double);
+    if (nk > 0 && ne > 0) {
+        const int64_t nb = ne + nk + 2, nb4 = round_up(nb, 4);
+        bytes += 2 * 4 * round_up(ne, kChunk) + 4 * 4 * round_up(nk, kChunk) + 4 * nb4;
+        const int64_t trace = nb4 * kSlots;
+        if (trace_budget > 0 && trace > trace_budget)
+            bytes += 4 * (nb / kCkBands + 1) * kCkStride + (int64_t)kCkBands * kSlots;
+        else
+            bytes += trace;
+        if (scores) bytes += 4 * (int64_t)kSlots * nb4;
+    }
+    return bytes;
+}
+
+static int64_t slab_fixed_bytes() {
+    return (int64_t)sizeof(abea_model_t) * ABEA_NUM_KMER + 2 * (int64_t)sizeof(double) * ABEA_NUM_KMER +
+           32 * 256 + 16 * 1024;
+}
+
+static void CUDART_CB stamp_now(void* p) {
+    *(std::chrono::steady_clock::time_point*)p = std::chrono::steady_clock::now();
+}
+
+namespace {
+// One of the two device batches of a stream: its inputs rebased to the batch.
+struct StreamSlot {
+    abea_batch* b = nullptr;
+    cudaEvent_t* ev = nullptr;  // uploaded, compute start, compute end, results copied
+    std::vector<int64_t> rp, ep;
+    int32_t r0 = 0, r1 = 0;
+    int64_t ev_base = 0;
+    bool busy = false;  // work of its last batch is queued
+};
+}  // namespace
+
+extern "C" abea_status_t abea_align_stream(abea_ctx_t* c, const abea_stream_config_t* cfg, int32_t n_reads,
+                                           const char* read, const int64_t* read_ptr, const int32_t* read_len,
+                                           const abea_event_t* event_table, const int64_t* event_ptr,
+                                           const int32_t* n_events, const abea_scalings_t* scalings,
+                                           const abea_model_t* model, abea_aligned_pair_t* pairs,
+                                           int32_t* n_pairs, abea_scalings_t* scalings_out, double* latency_ms,
+                                           abea_stream_stats_t* stats) {
+    using clock = std::chrono::steady_clock;
+    const clock::time_point t_call = clock::now();
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_align_stream: null context");
+    if (n_reads > 0 && (!pairs || !n_pairs)) return fail(ABEA_ERR_INVALID_ARG, "abea_align_stream: null output");
+    const abea_stream_config_t conf = cfg ? *cfg : abea_stream_config_t{0, 0, 0};
+    if (conf.batch_bytes < 0 || conf.recalibrate < 0 || conf.recalibrate > 1 || conf.reserved != 0)
+        return fail(ABEA_ERR_INVALID_ARG, "abea_align_stream: bad configuration");
+    const HostInputs all = inputs(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model);
+    abea_status_t st = validate(all);
+    if (st) return st;
+    for (int32_t i = 0; i + 1 < n_reads; ++i)
+        if (event_ptr[i] + n_events[i] > event_ptr[i + 1])
+            return fail(ABEA_ERR_INVALID_ARG, "abea_align_stream: event ranges of reads %d and %d overlap or are out of order",
+                        i, i + 1);
+    if (stats) *stats = abea_stream_stats_t{};
+    if (n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    int64_t budget = conf.batch_bytes;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+        budget = std::min<int64_t>(16ll << 30, (int64_t)(0.4 * (double)fr));
+    }
+    // admission in input order by device footprint
+    const bool scores = c->store_scores != 0;
+    std::vector<int32_t> cut = {0};
+    std::vector<int64_t> cut_bytes;
+    int64_t acc = slab_fixed_bytes(), max_bytes = 0, cells = 0;
+    for (int32_t i = 0; i < n_reads; ++i) {
+        const int64_t rb = read_device_bytes(read_len[i], n_events[i], c->trace_budget, scores);
+        if (i > cut.back() && acc + rb > budget) {
+            cut.push_back(i);
+            cut_bytes.push_back(acc);
+            max_bytes = std::max(max_bytes, acc);
+            acc = slab_fixed_bytes();
+        }
+        acc += rb;
+        const int64_t nk = (int64_t)read_len[i] - ABEA_KMER_SIZE + 1;
+        if (nk > 0 && n_events[i] > 0) cells += (n_events[i] + nk + 2) * (int64_t)kBand;
+    }
+    cut.push_back(n_reads);
+    cut_bytes.push_back(acc);
+    max_bytes = std::max(max_bytes, acc);
+    const int nb = (int)cut.size() - 1;
+    // resources kept by the context
+    if (!c->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; ++i) {
+        if (!c->sslot[i]) {
+            c->sslot[i] = new (std::nothrow) abea_batch();
+            if (!c->sslot[i]) return fail(ABEA_ERR_OUT_OF_MEMORY, "host allocation failed");
+            c->sslot[i]->ctx = c;
+        }
+        for (int j = 0; j < 4; ++j)
+            if (!c->sev[i][j]) CUDA_TRY(cudaEventCreate(&c->sev[i][j]));
+    }
+    int32_t* status = nullptr;
+    if (cudaHostAlloc((void**)&status, sizeof(int32_t) * (size_t)n_reads, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ABEA_ERR_OUT_OF_MEMORY, "pinned status array failed");
+    }
+    StreamSlot slot[2];
+    for (int i = 0; i < 2; ++i) {
+        slot[i].b = c->sslot[i];
+        slot[i].ev = c->sev[i];
+    }
+    std::vector<clock::time_point> admit((size_t)nb), done((size_t)nb);
+    cudaStream_t cs = c->copy_stream;
+    double compute_ms = 0;
+    int32_t max_reads = 0;
+    std::vector<abea_scalings_t> sc;
+    std::vector<double> gn;
+    std::vector<int32_t> ast;
+
+    auto harvest = [&](StreamSlot& S) -> abea_status_t {  // the slot's last batch is done
+        if (!S.busy) return ABEA_OK;
+        CUDA_TRY(cudaEventSynchronize(S.ev[3]));
+        float ms = 0;
+        CUDA_TRY(cudaEventElapsedTime(&ms, S.ev[1], S.ev[2]));
+        compute_ms += ms;
+        S.busy = false;
+        return ABEA_OK;
+    };
+    auto prepare = [&](int k) -> abea_status_t {  // admit batch k: plan and copy to the device
+        StreamSlot& S = slot[k & 1];
+        abea_status_t s2 = harvest(S);
+        if (s2) return s2;
+        S.r0 = cut[(size_t)k];
+        S.r1 = cut[(size_t)k + 1];
+        const int32_t n = S.r1 - S.r0;
+        max_reads = std::max(max_reads, n);
+        int64_t rbase = read_ptr[S.r0];
+        for (int32_t i = S.r0; i < S.r1; ++i) rbase = std::min(rbase, read_ptr[i]);
+        S.ev_base = event_ptr[S.r0];
+        S.rp.resize((size_t)n);
+        S.ep.resize((size_t)n);
+        for (int32_t i = 0; i < n; ++i) {
+            S.rp[(size_t)i] = read_ptr[S.r0 + i] - rbase;
+            S.ep[(size_t)i] = event_ptr[S.r0 + i] - S.ev_base;
+        }
+        HostInputs in = inputs(n, read + rbase, S.rp.data(), read_len + S.r0,
+                               event_table ? event_table + S.ev_base : nullptr, S.ep.data(), n_events + S.r0,
+                               scalings + S.r0, model);
+        if ((s2 = plan(S.b, in, (int)c->var_aware, c->trace_budget)) ||
+            (s2 = ensure_device(S.b, scores, (size_t)max_bytes)))
+            return s2;
+        prepare_order(c, S.b);
+        admit[(size_t)k] = clock::now();
+        if ((s2 = upload(S.b, in, cs))) return s2;
+        if (c->mode == ABEA_MODE_BATCHED) {  // the batched form's order, so that the run needs no copy
+            CUDA_TRY(cudaMemcpyAsync(S.b->d_order, S.b->dev_order.data(), sizeof(int32_t) * S.b->dev_order.size(),
+                                     cudaMemcpyHostToDevice, cs));
+            S.b->dev_order_sent = S.b->dev_order;
+        }
+        CUDA_TRY(cudaEventRecord(S.ev[0], cs));
+        S.busy = true;
+        return ABEA_OK;
+    };
+    auto start = [&](int k) -> abea_status_t {  // align batch k
+        StreamSlot& S = slot[k & 1];
+        CUDA_TRY(cudaStreamWaitEvent(c->stream, S.ev[0], 0));
+        CUDA_TRY(cudaEventRecord(S.ev[1], c->stream));
+        return run_batch(c, S.b);
+    };
+    auto finish = [&](int k) -> abea_status_t {  // recalibrate, re-align, copy the results back
+        StreamSlot& S = slot[k & 1];
+        abea_batch* b = S.b;
+        const size_t n = (size_t)b->n_reads;
+        abea_status_t s2;
+        if (conf.recalibrate) {
+            if ((s2 = queue_backward(c, b, false))) return s2;
+            gn.resize(5 * n);
+            ast.resize(n);
+            CUDA_TRY(cudaMemcpyAsync(gn.data(), b->d_gn, sizeof(double) * 5 * n, cudaMemcpyDeviceToHost, c->stream));
+            CUDA_TRY(cudaMemcpyAsync(ast.data(), b->d_adj_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                     c->stream));
+            CUDA_TRY(cudaStreamSynchronize(c->stream));
+            sc.resize(n);
+            for (size_t i = 0; i < n; ++i) {
+                const ReadDesc& r = b->reads[i];
+                sc[i] = abea_scalings_t{r.scale, r.shift, r.var, r.log_var};
+            }
+            gn_step(b, gn.data(), ast.data(), sc.data());
+            apply_scalings(b, sc.data());
+            if ((s2 = upload_reads(c, b)) || (s2 = run_batch(c, b))) return s2;
+        }
+        if (scalings_out)
+            for (size_t i = 0; i < n; ++i) {
+                const ReadDesc& r = b->reads[i];
+                scalings_out[S.r0 + i] = abea_scalings_t{r.scale, r.shift, r.var, r.log_var};
+            }
+        CUDA_TRY(cudaEventRecord(S.ev[2], c->stream));
+        CUDA_TRY(cudaStreamWaitEvent(cs, S.ev[2], 0));
+        if (b->pair_cap > 0)
+            CUDA_TRY(cudaMemcpyAsync(pairs + 2 * S.ev_base, b->d_pairs, sizeof(abea_aligned_pair_t) * (size_t)b->pair_cap,
+                                     cudaMemcpyDeviceToHost, cs));
+        CUDA_TRY(cudaMemcpyAsync(n_pairs + S.r0, b->d_n_pairs, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, cs));
+        CUDA_TRY(cudaMemcpyAsync(status + S.r0, b->d_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, cs));
+        CUDA_TRY(cudaEventRecord(S.ev[3], cs));
+        CUDA_TRY(cudaLaunchHostFunc(cs, stamp_now, &done[(size_t)k]));
+        return ABEA_OK;
+    };
+
+    st = prepare(0);
+    for (int k = 0; k < nb && !st; ++k) {
+        if ((st = start(k))) break;
+        if (k + 1 < nb && (st = prepare(k + 1))) break;  // overlaps batch k's alignment
+        st = finish(k);
+    }
+    // drain both streams before returning (copies into the caller's buffers)
+    const cudaError_t e1 = cudaStreamSynchronize(c->stream), e2 = cudaStreamSynchronize(cs);
+    if (!st && e1 != cudaSuccess) st = fail(ABEA_ERR_CUDA, "stream: %s", cudaGetErrorString(e1));
+    if (!st && e2 != cudaSuccess) st = fail(ABEA_ERR_CUDA, "stream: %s", cudaGetErrorString(e2));
+    for (int i = 0; i < 2 && !st; ++i) st = harvest(slot[i]);
+    for (int i = 0; i < 2; ++i) slot[i].busy = false;
+    if (!st) {
+        for (int32_t i = 0; i < n_reads; ++i)
+            if (status[i] != 0) {
+                st = fail((abea_status_t)status[i], "read %d: %s", i, abea_status_string((abea_status_t)status[i]));
+                break;
+            }
+    }
+    cudaFreeHost(status);
+    if (st) return st;
+    clock::time_point last = t_call;
+    for (int k = 0; k < nb; ++k) {
+        last = std::max(last, done[(size_t)k]);
+        if (latency_ms) {
+            const double ms = std::chrono::duration<double, std::milli>(done[(size_t)k] - admit[(size_t)k]).count();
+            for (int32_t i = cut[(size_t)k]; i < cut[(size_t)k + 1]; ++i) latency_ms[i] = ms;
+        }
+    }
+    if (stats) {
+        stats->n_batches = nb;
+        stats->max_batch_reads = max_reads;
+        stats->max_batch_bytes = max_bytes;
+        stats->band_cells = cells;
+        stats->wall_ms = std::chrono::duration<double, std::milli>(last - t_call).count();
+        stats->compute_ms = compute_ms;
     }
     return ABEA_OK;
 }

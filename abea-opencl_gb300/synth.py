@@ -54,13 +54,14 @@ def kmer_ranks(seq: np.ndarray) -> np.ndarray:
     return r
 
 
-def read_lengths(rng: np.random.Generator, workload: str) -> np.ndarray:
+def read_lengths(rng: np.random.Generator, workload: str, target=None) -> np.ndarray:
     if workload == "small":
         return rng.integers(1000, 3001, 64)
     if workload == "adjoint":
         return rng.integers(1000, 10001, 4096)
     if workload in ("f5c_batch", "uneven", "serving"):
-        target = 200_000_000 if workload == "serving" else 1_300_000
+        if target is None:
+            target = 200_000_000 if workload == "serving" else 1_300_000
         lens = []
         total = 0
         while total < target:
@@ -141,4 +142,92 @@ def make_batch(workload: str = "small", seed: int = 1, perturb: bool = False, le
         model=model,
         meta={"workload": workload, "seed": seed, "true_scalings": true_sc,
               "sample_rate": SAMPLE_RATE, "lognormal_sigma": LOGNORMAL_SIGMA},
+    )
+
+
+
+def _stream_chunk(seed_seq, model, lens, sc):
+    """Sequences and events of one chunk of reads (make_stream)."""
+    rng = np.random.default_rng(seed_seq)
+    L = lens.astype(np.int64)
+    m = len(L)
+    tot = int(L.sum())
+    starts = np.zeros(m, dtype=np.int64)
+    starts[1:] = np.cumsum(L[:-1])
+    codes = rng.integers(0, 4, tot).astype(np.uint8)
+    seq = _BASES[codes]
+    # k-mer ranks at every position; drop the ones that cross a read's end
+    nw = tot - KMER_SIZE + 1
+    r = np.zeros(nw, dtype=np.int32)
+    for j in range(KMER_SIZE):
+        r = (r << 2) | codes[j:j + nw]
+    valid = np.ones(nw, dtype=bool)
+    tail = ((starts + L)[:, None] - KMER_SIZE + 1 + np.arange(KMER_SIZE - 1)[None, :]).ravel()
+    valid[tail[tail < nw]] = False
+    ranks = r[valid]
+    kread = np.repeat(np.arange(m, dtype=np.int32), L - KMER_SIZE + 1)
+    counts = rng.geometric(1.0 / 1.8, len(ranks))
+    counts[rng.random(len(ranks)) < 0.05] = 0
+    kidx = np.repeat(np.arange(len(ranks), dtype=np.int64), counts)
+    rk = ranks[kidx]
+    eread = kread[kidx]
+    ne = len(kidx)
+    ev = np.zeros(ne, dtype=EVENT_DTYPE)
+    mu = (model["level_mean"].astype(np.float64)[rk] * sc["scale"].astype(np.float64)[eread]
+          + sc["shift"].astype(np.float64)[eread])
+    sd = model["level_stdv"].astype(np.float64)[rk] * 1.2
+    ev["mean"] = (mu + rng.standard_normal(ne) * sd).astype(np.float32)
+    length_s = np.minimum(3 + rng.geometric(0.5, ne) - 1, 34)
+    ev["length"] = length_s.astype(np.float32)
+    cnt = np.bincount(eread, minlength=m).astype(np.int32)
+    first = np.zeros(m, dtype=np.int64)
+    first[1:] = np.cumsum(cnt[:-1])
+    excl = np.cumsum(length_s) - length_s
+    ev["start"] = (excl - excl[first[eread]]).astype(np.uint64)
+    ev["stdv"] = (model["level_stdv"][rk] * rng.uniform(0.8, 1.2, ne)).astype(np.float32)
+    return seq, starts, ev, cnt
+
+
+def make_stream(seed: int = 1, total_bases: int = 200_000_000, chunk_reads: int = 512, threads=None) -> Batch:
+    """The serving workload (lognormal lengths, median 8 kb, clipped to
+    [500, 200000], `total_bases` in all) with the laws of make_read, generated a
+    chunk of reads at a time with array operations, chunks on a thread pool, each
+    chunk from its own child seed (the result does not depend on `threads`; the
+    random stream differs from make_batch's)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    rng = np.random.default_rng(np.random.SeedSequence(seed, spawn_key=(0,)))
+    model = make_model(rng)
+    lens = read_lengths(rng, "serving", target=total_bases)
+    n = len(lens)
+    true_sc = np.zeros(n, dtype=SCALINGS_DTYPE)
+    true_sc["scale"] = rng.normal(1.0, 0.05, n).astype(np.float32)
+    true_sc["shift"] = rng.normal(0.0, 5.0, n).astype(np.float32)
+    true_sc["var"] = np.float32(1.2)
+    true_sc["log_var"] = np.float32(np.log(1.2))
+    read_ptr = np.zeros(n, dtype=np.int64)
+    read_ptr[1:] = np.cumsum(lens[:-1] + 1)
+    read = np.zeros(int(lens.sum()) + n, dtype=np.uint8)
+    bounds = list(range(0, n, chunk_reads))
+    chunk_seeds = np.random.SeedSequence(seed, spawn_key=(1,)).spawn(len(bounds))
+    with ThreadPoolExecutor(max_workers=threads or min(16, os.cpu_count() or 1)) as pool:
+        parts = list(pool.map(lambda k: _stream_chunk(chunk_seeds[k], model, lens[bounds[k]:bounds[k] + chunk_reads],
+                                                      true_sc[bounds[k]:bounds[k] + chunk_reads]),
+                              range(len(bounds))))
+    n_events = np.zeros(n, dtype=np.int32)
+    for k, (seq, starts, _, cnt) in enumerate(parts):
+        a = bounds[k]
+        n_events[a:a + len(cnt)] = cnt
+        for j in range(len(cnt)):  # NUL-separated, as make_batch lays them out
+            p = read_ptr[a + j]
+            read[p:p + lens[a + j]] = seq[starts[j]:starts[j] + lens[a + j]]
+    event_ptr = np.zeros(n, dtype=np.int64)
+    if n:
+        event_ptr[1:] = np.cumsum(n_events[:-1].astype(np.int64))
+    events = np.concatenate([p[2] for p in parts]) if parts else np.zeros(0, dtype=EVENT_DTYPE)
+    return Batch(
+        read=read, read_ptr=read_ptr, read_len=lens.astype(np.int32), events=events, event_ptr=event_ptr,
+        n_events=n_events, scalings=true_sc.copy(), model=model,
+        meta={"workload": "serving", "seed": seed, "true_scalings": true_sc, "sample_rate": SAMPLE_RATE,
+              "lognormal_sigma": LOGNORMAL_SIGMA, "total_bases": int(lens.sum())},
     )

@@ -292,6 +292,49 @@ abea_status_t abea_batch_recalibrate(abea_ctx_t *ctx, abea_batch_t *batch, int32
 abea_status_t abea_batch_estimate_scalings(abea_ctx_t *ctx, abea_batch_t *batch, abea_scalings_t *out,
                                            int32_t apply);
 
+/* ---- serving stream (no counterpart in the reference) --------------------
+ * A stream of reads in the batch layout of abea_align_batch, admitted in input
+ * order into device batches whose device footprint (sequence, events, k-mer
+ * tables, trace or checkpoints, outputs) stays under `batch_bytes`.  Two
+ * batches are in flight: batch i+1 is copied to the device on a second stream
+ * while batch i runs on the context's stream, and batch i's results go back on
+ * that second stream.  Per batch: the alignment and, with `recalibrate`, the
+ * adjoint, one Gauss-Newton step of every read's (shift, scale) and the
+ * re-alignment with the new scalings (whose AlignedPairs are the ones returned).
+ * A read larger than `batch_bytes` forms a batch of its own. */
+typedef struct {
+    int64_t batch_bytes;  /* device footprint limit of one batch; 0 = the smaller of 16 GiB and
+                             40% of the device's free memory */
+    int32_t recalibrate;  /* 0 = align; 1 = align, adjoint, one Gauss-Newton step, re-align */
+    int32_t reserved;     /* 0 */
+} abea_stream_config_t;
+
+typedef struct {
+    int32_t n_batches;
+    int32_t max_batch_reads;
+    int64_t max_batch_bytes;  /* largest device footprint of one batch */
+    int64_t band_cells;       /* sum of n_bands*100 over the reads (each read once) */
+    double wall_ms;           /* from the call to the last batch's results in host memory */
+    double compute_ms;        /* sum of the batches' device time on the context's stream */
+} abea_stream_stats_t;
+
+/* Inputs and outputs as abea_align_batch, with reads whose event ranges follow
+ * one another (event_ptr[i] + n_events[i] <= event_ptr[i+1]).  Host buffers from
+ * abea_host_alloc let the copies overlap the alignment; pageable buffers work but
+ * their copies wait for the device.  Outputs (each may be NULL except the pairs
+ * and counts): scalings_out[n_reads] the scalings each read was finally aligned
+ * with; read_latency_ms[n_reads] the time from the admission of the read's batch
+ * (the host queuing its copy to the device) to its results being in host memory;
+ * stats.  Returns the first failing read's status after every batch has run,
+ * like abea_align_batch. */
+abea_status_t abea_align_stream(abea_ctx_t *ctx, const abea_stream_config_t *cfg, int32_t n_reads,
+                                const char *read, const int64_t *read_ptr, const int32_t *read_len,
+                                const abea_event_t *event_table, const int64_t *event_ptr,
+                                const int32_t *n_events, const abea_scalings_t *scalings,
+                                const abea_model_t *model, abea_aligned_pair_t *event_align_pairs,
+                                int32_t *n_event_align_pairs, abea_scalings_t *scalings_out,
+                                double *read_latency_ms, abea_stream_stats_t *stats);
+
 /* ---- no-allocation entry point ------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory themselves or through this library: a framework whose own allocator

@@ -209,3 +209,16 @@ def test_autotuned_batched_stays_exact(lib, oracle_mod):
     assert dev.timing()["kernel_launches"] == 2  # pre + fused core/post, one graph
     op, oc, _ = oracle_batch(oracle_mod, batch)
     assert_same_alignments(batch, gp, gc, op, oc)
+
+
+def test_graph_recaptured_for_each_batch_layout(lib, oracle_mod):
+    """abea_align_batch reuses one device batch per context: a second batch with
+    the same read count but other lengths carves the device slab differently, so
+    the batched form's graph must not replay the first batch's pointers."""
+    from abea_gb300 import synth
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    for lengths in ([1500, 2600, 1200, 900], [2900, 700, 2200, 1800], [1500, 2600, 1200, 900]):
+        batch = synth.make_batch("small", seed=len(lengths) + lengths[1], lengths=lengths)
+        gp, gc = ctx.align_batch(batch)
+        op, oc, _ = oracle_batch(oracle_mod, batch)
+        assert_same_alignments(batch, gp, gc, op, oc)
