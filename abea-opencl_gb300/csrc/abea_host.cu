@@ -130,6 +130,7 @@ struct abea_ctx {
     int64_t spin_limit = 1 << 22;
     int64_t var_aware = 0;
     int64_t trace_budget = 0;  // bytes of trace a read may keep (0 = every trace)
+    int64_t wide_cluster = 0;  // batched form: wide reads on a cluster pair of blocks
     void* db_pin = nullptr;    // pinned staging of abea_align_db
     size_t db_pin_bytes = 0;
     int sm_count = 0;
@@ -233,6 +234,7 @@ extern "C" abea_status_t abea_ctx_set_option(abea_ctx_t* c, abea_option_t opt, i
         if (v < 0) return fail(ABEA_ERR_INVALID_ARG, "trace budget must be >= 0");
         c->trace_budget = v;
         return ABEA_OK;
+    case ABEA_OPT_WIDE_CLUSTER: c->wide_cluster = v != 0; return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -247,6 +249,7 @@ extern "C" abea_status_t abea_ctx_get_option(abea_ctx_t* c, abea_option_t opt, i
     case ABEA_OPT_SPIN_LIMIT: *v = c->spin_limit; return ABEA_OK;
     case ABEA_OPT_VAR_AWARE: *v = c->var_aware; return ABEA_OK;
     case ABEA_OPT_TRACE_BUDGET: *v = c->trace_budget; return ABEA_OK;
+    case ABEA_OPT_WIDE_CLUSTER: *v = c->wide_cluster; return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -526,8 +529,8 @@ static int64_t d2h_bytes(const abea_batch* b) {
 // evenly over the resident warps (their warp-shape fill would outlast the rest
 // of the batch), at most one per resident block, never a checkpointed read.
 // Fills b->dev_order with those reads first, then the rest longest first.
-static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, bool scores) {
-    const int blocks = batched_blocks_per_sm(scores) * sm_count;
+static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, bool scores, bool cluster) {
+    const int blocks = cluster ? sm_count / 2 : batched_blocks_per_sm(scores) * sm_count;
     int64_t total = 0;
     for (const ReadDesc& r : b->reads) total += r.n_bands;
     if (threshold <= 0) threshold = std::max<int64_t>(1, total / std::max(1, blocks * 8));
@@ -552,7 +555,8 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
                      b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col};
     la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
                        b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
-                       b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch};
+                       b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch,
+                       (long long)c->spin_limit};
     la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1, b->d_km_rsd,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
                        b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event};
@@ -561,6 +565,7 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
     la.ev_pre = c->ev[1];
     la.ev_core = c->ev[2];
     la.capturing = capturing;
+    la.cluster = c->wide_cluster != 0;
     cudaError_t e = c->mode == ABEA_MODE_BATCHED ? launch_batched(la, launches) : launch_plain(la, launches);
     if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
     return ABEA_OK;
@@ -596,7 +601,7 @@ static void prepare_order(abea_ctx* c, abea_batch* b) {
         auto it = c->tuned.find(workload_signature(b));
         if (it != c->tuned.end()) thr = it->second;
     }
-    b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept);
+    b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept, c->wide_cluster != 0);
 }
 
 static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
@@ -624,7 +629,8 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
         std::vector<uint64_t> key = b->carve;
         key.push_back((uint64_t)b->n_reads);
         key.push_back((uint64_t)b->n_wide);
-        key.push_back((uint64_t)(b->scores_kept ? 1 : 0) | ((uint64_t)b->var_aware << 1));
+        key.push_back((uint64_t)(b->scores_kept ? 1 : 0) | ((uint64_t)b->var_aware << 1) |
+                      ((uint64_t)(c->wide_cluster != 0) << 2));
         if (!b->graph || key != b->graph_key) {
             if (b->graph) cudaGraphExecDestroy(b->graph);
             b->graph = nullptr;
@@ -734,6 +740,10 @@ static abea_status_t download(abea_ctx* c, abea_batch* b, abea_aligned_pair_t* p
 
 static abea_status_t check_status(abea_ctx* c, abea_batch* b) {
     if (b->n_reads == 0) return ABEA_OK;
+    unsigned long long cnt[4] = {0, 0, 0, 0};
+    CUDA_TRY(cudaMemcpyAsync(cnt, b->d_slow, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (cnt[2]) return fail(ABEA_ERR_TIMEOUT, "%llu device-side waits ran out of polls (ABEA_OPT_SPIN_LIMIT)", cnt[2]);
     std::vector<int32_t> st((size_t)b->n_reads);
     CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_status, sizeof(int32_t) * st.size(), cudaMemcpyDeviceToHost,
                              c->stream));

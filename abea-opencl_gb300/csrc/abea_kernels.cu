@@ -24,6 +24,7 @@
 //             longest reads on the wide shape, then its warps pull the remaining
 //             reads longest-first from a device queue; every read's post runs in
 //             the warp that filled it, right after its fill (trace still in L2).
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -741,6 +742,371 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     wide_barrier();
 }
 
+// ---------------------------------------------------------------- wide shape on a cluster pair
+// The wide fill with its emission work on a second SM: blocks run in clusters
+// of two.  The cluster's first block holds the read's band state and runs three
+// groups of 128 threads (B: the band-to-band chain, D: diagonal candidates and
+// inside flags, K: bookkeeping and the prefetch rings of the FP64 slow path).
+// The second block's four groups compute the emissions and their exact splits,
+// group g the bands 2+g, 6+g, ..., stage them in their own shared memory and
+// bulk-copy them into the first block's (distributed shared memory) up to
+// kClRing bands ahead of the chain; one mbarrier per ring slot counts a band's
+// bytes.  D waits on it before it prepares the band's diagonal candidates, and
+// the block barrier that follows hands the band to B.
+// A band's cells lie on one anti-diagonal (event + k-mer = band - 2), so the
+// emissions of band bn only need a k-mer window that holds the band: the
+// placement k0 of any earlier band p with bn - p <= 28 gives one, [k0, k0+128),
+// because each band moves k0 by at most one.  The first block publishes its
+// progress, with the placement of the band it names, into the second block's
+// shared memory every kClPublish bands (each release is a cluster-scope fence:
+// once per band they cost ~400 cycles per band).  E reads its inputs straight
+// from the pre stage's arrays (L2), one band ahead.  Every wait is bounded by
+// spin_limit polls; a wait that runs out counts in counters[2] and goes on (the
+// batch then reports a timeout).  Measured: 1,030 cycles per band against 600
+// for the single-block wide shape, so the option is off by default.
+constexpr int kClRing = 16;    // bands of emissions in flight (<= 28: the k-mer window above)
+constexpr int kClPublish = 8;  // block 0 publishes its progress every kClPublish bands (< kClRing)
+
+struct alignas(16) ClSmem {
+    Rings rg;                                   // block 0: rings of the FP64 slow path
+    float sc[2][kSlots];
+    // written by block 1, per band slot and k-mer slot: {pstay, wstay, magu, em} and {pstep, wstep}
+    float4 emu[kClRing][kSlots];
+    float2 emd[kClRing][kSlots];
+    float dc[2][kSlots];
+    int32_t flags[2][kSlots];
+    float trim[2];
+    uint32_t fr[8][kSlots];
+    int32_t k0h[8];
+};
+
+// Cluster state that outlives the fill (the fill's shared memory is reused
+// afterwards; the mbarriers and the partner's stores must not land there).
+struct ClShared {
+    uint64_t full[kClRing];  // block 0: band b's emissions in slot (b-2) % kClRing have landed
+                             // (phase (b-2) / kClRing of that slot's mbarrier)
+    int32_t k0ring[64];      // block 1: placement of band b at [b & 63], from block 0
+    int32_t progress;        // block 1: block 0 is done with the emissions of bands <= progress
+    int32_t pick;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Waits for the phase of parity `parity` of a local mbarrier, at most limit/64
+// polls (each poll may itself suspend the thread for a while); false when they
+// ran out.  CTA-scope acquire: the data that completes the phase (bulk copies
+// counted by complete_tx) is visible to the waiting thread once it observes the
+// completion, whichever block issued the copies.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, long long limit) {
+    const unsigned a = smem_u32(bar);
+    const long long polls = limit > 0 ? (limit >> 6) + 1 : 0;
+    for (long long i = 0; i < polls; ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Remote shared-memory address of `p`'s counterpart in block `rank`.
+__device__ __forceinline__ unsigned mapa_u32(const void* p, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    return r;
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// this block's shared memory to another block's (remote address `rdst`),
+// counted on that block's mbarrier `rbar` (complete_tx).
+__device__ __forceinline__ void bulk_to_remote(unsigned rdst, const void* src, unsigned bytes, unsigned rbar) {
+    asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     rdst),
+                 "r"(smem_u32(src)), "r"(bytes), "r"(rbar)
+                 : "memory");
+}
+
+// One arrival on block `rank`'s mbarrier that also expects `bytes` of
+// complete_tx stores in the current phase.
+__device__ __forceinline__ void mbar_arrive_expect_remote(unsigned rbar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cluster.shared::cluster.b64 _, [%0], %1;\n" ::"r"(rbar),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Release store of v to the int at the same place in block `rank`.
+__device__ __forceinline__ void st_release_remote(int32_t* p, unsigned rank, int32_t v) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    asm volatile("st.release.cluster.shared::cluster.u32 [%0], %1;\n" ::"r"(r), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int32_t ld_acquire_local(const int32_t* p) {
+    int32_t v;
+    asm volatile("ld.acquire.cluster.shared::cta.u32 %0, [%1];\n" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void cl_barrier() { asm volatile("bar.sync 1, 384;\n" ::: "memory"); }
+__device__ __forceinline__ void e_barrier(int group) { asm volatile("bar.sync %0, 128;\n" ::"r"(2 + group) : "memory"); }
+// Called by every thread of both blocks of the cluster (rank = block rank).
+template <bool kScores>
+__device__ void fill_wide_cl(const CoreArgs& a, const ReadDesc& r, ClSmem& ws, ClShared& cs, int tid,
+                             unsigned rank) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const CellConsts cc = make_consts(r, a.g);
+    const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
+    const int group = tid >> 7;  // block 0: 0 = B, 1 = D, 2 = K, 3 = idle; block 1: E groups 0-3
+    const int t = tid & (kSlots - 1);
+    const long long lim = a.spin_limit;
+    unsigned long long timeouts = 0;
+    bool dead = false;  // a wait ran out: later waits do not wait (the batch reports a timeout)
+
+    int k0 = -1 - kBand / 2, e0 = kBand / 2;  // band 1 (band 0 is (49,-51), band 1 moved down)
+    RingState rs;
+    if (rank == 0 && group == 2) rings_init(ws.rg, rs, a, r, t, k0, e0);
+    if (rank == 0 && tid == 0) {
+        for (int i = 0; i < kClRing; ++i) mbar_init(&cs.full[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (rank == 1 && tid == 0) {
+        cs.k0ring[1] = k0;
+        cs.progress = 1;
+    }
+    cluster.sync();  // barriers initialised, progress 1 published, rings filled
+
+    if (rank == 1) {
+        // ------------------------------------------------ E (block 1): group g, bands 2+g, 6+g, ...
+        const float* gm_p = a.km_gm + r.km_off;
+        const float* sd_p = a.km_sd + r.km_off;
+        const float* rsd_p = a.km_rsd + r.km_off;
+        const float* k1_p = a.km_k1 + r.km_off;
+        const float* ev_p = a.ev_mean + r.ev_off;
+        struct In {
+            float x, gm, sd, rsd, k1;
+        };
+        // band bn's inputs in slot t, k-mer window from the latest published placement;
+        // waits until that placement is at most kClRing bands back (its ring slot is free)
+        auto fetch = [&](int bn) {
+            int prog = ld_acquire_local(&cs.progress);
+            for (long long i = 0; prog < bn - kClRing && i < (dead ? 0 : lim); ++i)
+                prog = ld_acquire_local(&cs.progress);
+            if (prog < bn - kClRing) {
+                ++timeouts;
+                dead = true;
+            }
+            const int kp = cs.k0ring[prog & 63];
+            const int kk = kp + ((t - kp) & 127);
+            const int e = bn - 2 - kk;
+            // cells outside the read get finite stand-ins; their flags keep them out of the band
+            const bool in = kk >= 0 && kk < n_kmers && e >= 0 && e < n_events;
+            const int kc = in ? kk : 0, ec = in ? e : 0;
+            return In{__ldg(ev_p + ec), __ldg(gm_p + kc), __ldg(sd_p + kc), __ldg(rsd_p + kc), __ldg(k1_p + kc)};
+        };
+        int bn = 2 + group;
+        In cur = bn < n_bands ? fetch(bn) : In{0.0f, 0.0f, 1.0f, 1.0f, 0.0f};
+        for (; bn < n_bands; bn += 4) {
+            bool ok;
+            const float em = emission_fast(cur.x, cur.gm, cur.sd, cur.rsd, cur.k1, ok);
+            const EmSplit s1 = em_split(em, cc.step_h, cc.step_l);
+            const EmSplit s2 = em_split(em, cc.stay_h, cc.stay_l);
+            if (bn + 4 < n_bands) cur = fetch(bn + 4);  // loads in flight across the stores
+            // staged in this block's own copy of the slot (free: the band kClRing back
+            // was consumed, so its copy has been read), then one bulk copy per array
+            const int s = (bn - 2) % kClRing;
+            ws.emu[s][t] = make_float4(s2.p, s2.w,
+                                       ok ? __fadd_rn(fabsf(em), fabsf(cc.stay_h)) : __int_as_float(0x7fc00000), em);
+            ws.emd[s][t] = make_float2(s1.p, s1.w);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // visible to the bulk copy
+            e_barrier(group);
+            if (t == 0) {
+                const unsigned rbar = mapa_u32(&cs.full[s], 0);
+                // one arrival and the band's 128 x 24 bytes complete the slot's phase
+                mbar_arrive_expect_remote(rbar, kSlots * 24);
+                bulk_to_remote(mapa_u32(&ws.emu[s][0], 0), &ws.emu[s][0], kSlots * 16, rbar);
+                bulk_to_remote(mapa_u32(&ws.emd[s][0], 0), &ws.emd[s][0], kSlots * 8, rbar);
+            }
+        }
+    } else if (group == 0) {
+        // ------------------------------------------------ B (block 0): the chain
+        ws.sc[1][t] = (t == 127) ? a.g.trim_f : -INFINITY;
+        ws.fr[0][t] = 0u;
+        ws.fr[1][t] = (t == 127) ? ABEA_FROM_U : 0u;
+        if (t == 0) {
+            ws.k0h[0] = k0;
+            ws.k0h[1] = k0;
+            a.band_k0[r.band_off] = k0;
+        }
+    }
+    if (rank == 0 && group < 3) {
+        cl_barrier();  // band 1 in shared memory
+        if (group == 0) {
+            float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
+            float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // band 1
+            float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
+            if (kScores) {
+                scores[t] = (t == 127) ? 0.0f : -INFINITY;
+                scores[kSlots + t] = s_prev;
+            }
+            unsigned long long slow = 0;
+            int b = 2, cb = 0;
+            float best = 0.0f, left = 0.0f;
+            uint32_t from = 0u;
+            bool valid = false, bad = false;
+            auto finish = [&]() {
+                best = valid ? best : -INFINITY;
+                from = valid ? from : 0u;
+                if (k0 <= -1) {  // trim cell (k = -1, slot 127) while the band reaches below k-mer 0
+                    const bool here = (t == 127) && (k0 >= -kBand);
+                    const float tv = ws.trim[cb];
+                    best = here ? tv : best;
+                    from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
+                }
+                ws.sc[cb][t] = best;
+                ws.fr[b & 7][t] = from;
+                if (kScores) scores[(int64_t)b * kSlots + t] = best;
+                lp = left;
+                s_prev = best;
+            };
+            while (true) {
+                bool to_slow = false;
+                for (; b < n_bands; ++b) {
+                    cl_barrier();  // B_{b-1}
+                    const int pb = (b - 1) & 1, es = (b - 2) % kClRing;
+                    cb = b & 1;
+                    // band b's emissions: D saw their mbarrier phase complete before the
+                    // barrier above (it prepared band b's diagonal candidates from them)
+                    const float ll = ws.sc[pb][k0 & 127];
+                    const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
+                    left = ws.sc[pb][(t + 127) & 127];
+                    const float d = ws.dc[cb][t];
+                    const int f = ws.flags[cb][t];
+                    const float4 eu = ws.emu[es][t];
+                    const EmSplit su{eu.x, eu.y};
+                    const float mu = eu.z;
+                    bool oku;
+                    const float u = exact_from_split(s_prev, su, mu, mu < INFINITY, oku);
+                    const bool right = band_moves_right(ll, ur, b);
+                    k0 += right ? 1 : 0;
+                    e0 += right ? 0 : 1;
+                    valid = (f & (right ? 2 : 1)) != 0;
+                    uint32_t from_du;
+                    const float best_du = pick_du(d, u, from_du);
+                    bool okl;
+                    const float l = exact_skip(left, cc.skip_h, cc.skip_l, okl);
+                    best = pick_l(best_du, from_du, l, from);
+                    bad = valid && !(oku && okl && (f & 4));
+                    if (__any_sync(kFull, bad)) {
+                        to_slow = true;
+                        break;
+                    }
+                    finish();
+                }
+                if (!to_slow) break;
+                if (bad) {  // a proof failed: the reference's FP64 arithmetic
+                    const int ep = e0 - ((t - k0) & 127);
+                    best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
+                                     ws.rg.k1[t], cc, from);
+                    ++slow;
+                }
+                finish();
+                ++b;
+            }
+            cl_barrier();  // B_{n_bands-1}
+            if (slow) atomicAdd(&a.counters[0], slow);
+        } else if (group == 1) {
+            // ------------------------------------------------ D (block 0)
+            // band bn's diagonal candidates, inside flags and trim value, with the
+            // band before it placed at k0
+            auto prep = [&](int bn, float diag) {
+                const int es = (bn - 2) % kClRing;
+                if (!mbar_wait(&cs.full[es], (unsigned)((bn - 2) / kClRing) & 1u, dead ? 0 : lim)) {
+                    ++timeouts;
+                    dead = true;
+                }
+                const float em = ws.emu[es][t].w;
+                const float2 ed = ws.emd[es][t];
+                const EmSplit s1{ed.x, ed.y};
+                bool okd;
+                const float d = exact_from_split(diag, s1, __fadd_rn(fabsf(em), fabsf(cc.step_h)),
+                                                 fabsf(em) < INFINITY, okd);
+                const int o = (t - k0) & 127;
+                const int kk = k0 + o;
+                const int e = bn - 2 - kk;
+                const bool inb = (kk >= 0) && (kk < n_kmers) && (e >= 0) && (e < n_events);
+                ws.dc[bn & 1][t] = d;
+                ws.flags[bn & 1][t] =
+                    ((inb && o < kBand) ? 1 : 0) | ((inb && o >= 1 && o <= kBand) ? 2 : 0) | (okd ? 4 : 0);
+                if (k0 <= 0 && t == 0) {  // trim cell of band bn (GPU/align_cuda.cl:431-443)
+                    const int e_t = bn - 1;
+                    ws.trim[bn & 1] =
+                        (e_t < n_events) ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
+                }
+            };
+            prep(2, (t == 0) ? 0.0f : -INFINITY);  // band 0 shifted by one slot
+            for (int b = 2; b < n_bands; ++b) {
+                cl_barrier();  // B_{b-1}
+                // B is done with the emissions of bands <= b-1, D with those of band b:
+                // E may reuse their ring slots; band b-1's placement was published with them
+                // (every kClPublish bands: each release is a cluster-scope fence)
+                if (t == 0 && (b & (kClPublish - 1)) == 0) st_release_remote(&cs.progress, 1, b - 1);
+                const int pb = (b - 1) & 1;
+                const float ll = ws.sc[pb][k0 & 127];
+                const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
+                const bool right = band_moves_right(ll, ur, b);
+                k0 += right ? 1 : 0;
+                if (t == 0) {
+                    ws.k0h[b & 7] = k0;
+                    // E reads the placement of the published band only (b - 1 at b a multiple of
+                    // kClPublish): written with the next progress store's release
+                    if (((b + 1) & (kClPublish - 1)) == 0) *cluster.map_shared_rank(&cs.k0ring[b & 63], 1) = k0;
+                }
+                if (b + 1 < n_bands) prep(b + 1, ws.sc[pb][(t + 127) & 127]);
+            }
+            cl_barrier();  // B_{n_bands-1}
+        } else if (group == 2) {
+            // ------------------------------------------------ K (block 0): bookkeeping, rings
+            uint8_t* trace = a.trace + r.trace_off * kSlots;
+            int32_t* bk0 = a.band_k0 + r.band_off;
+            float* lastc = a.last_col + r.ev_off;
+            const int sl_last = (n_kmers - 1) & 127;
+            for (int b = 2; b <= n_bands; ++b) {
+                cl_barrier();  // B_{b-1}
+                const int bp = b - 1;
+                const int kp = ws.k0h[bp & 7];
+                if ((b & 3) == 2) rings_step(ws.rg, rs, a, r, t, kp, bp - 2 - kp, 9);
+                const int ep0 = bp - 2 - kp;
+                const int ol = n_kmers - 1 - kp;
+                if (ol < kBand && t == sl_last && bp >= 2) {  // last k-mer column (GPU/align_cuda.cl:722-746)
+                    int lo, hi;
+                    band_range(kp, ep0, n_events, n_kmers, lo, hi);
+                    if (ol >= lo && ol < hi) lastc[ep0 - ol] = ws.sc[bp & 1][t];
+                }
+                if (t == 0) bk0[bp] = kp;
+                if ((bp & 3) == 3 || bp == n_bands - 1) {
+                    const int q0 = bp & ~3, nj = bp - q0;
+                    uint32_t word = 0u;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (j <= nj) word |= (ws.fr[(q0 + j) & 7][t] & 0xffu) << (8 * j);
+                    reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
+                }
+            }
+            cp_async_wait_all();
+        }
+    }
+    if (timeouts) atomicAdd(&a.counters[2], timeouts);
+}
+
 // ---------------------------------------------------------------- post
 struct alignas(16) PostSmem {
     uint8_t tr[4 * kPostChunkBands * kSlots];  // ring of 64 bands of trace, tile layout
@@ -1165,6 +1531,69 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
     }
 }
 
+struct BatchedClSmem {
+    union {
+        ClSmem wide;                       // phase 1: the cluster's wide read
+        Rings warp_rings[kBatchedWarps];   // then: one per warp
+    };
+    PostSmem post[kBatchedWarps];          // every warp's post staging
+    ClShared cs;
+};
+static_assert(offsetof(BatchedClSmem, warp_rings) % 16 == 0 && offsetof(BatchedClSmem, post) % 16 == 0,
+              "cp.async destinations must be 16-byte aligned");
+static_assert(sizeof(BatchedClSmem) <= 227 * 1024, "cluster kernel shared memory exceeds the per-block limit");
+
+// The batched form on clusters of two blocks: phase 1 fills one of the longest
+// reads per cluster with the cluster-pair wide shape, phase 2 as the
+// single-block kernel.
+template <bool kScores>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWideThreads, 1)
+    abea_batched_cl_kernel(CoreArgs a, PostArgs p) {
+    namespace cg = cooperative_groups;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BatchedClSmem& sm = *reinterpret_cast<BatchedClSmem*>(smem_raw);
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned rank = cluster.block_rank();
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    if (rank == 0 && t == 0) {
+        const int q = atomicAdd(&a.queue[0], 1);
+        const int pick = q < a.n_wide ? a.order[q] : -1;
+        sm.cs.pick = pick;
+        *cluster.map_shared_rank(&sm.cs.pick, 1) = pick;
+    }
+    cluster.sync();
+    const int wide_read = sm.cs.pick;
+    if (wide_read >= 0) {
+        const ReadDesc& r = a.reads[wide_read];
+        if (!r.skip) fill_wide_cl<kScores>(a, r, sm.wide, sm.cs, t, rank);
+        // every emission copy has landed (block 0 consumed them all) before either
+        // block reuses the fill's shared memory
+        cluster.sync();
+        __threadfence_block();
+        if (rank == 0 && warp == 0) post_read_warp(a, p, wide_read, sm.post[0], sm.warp_rings[0], lane);
+    }
+    // phase 2: every warp pulls reads longest-first
+    const int n_rest = a.n_reads - a.n_wide;
+    while (true) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(&a.queue[1], 1);
+        q = __shfl_sync(kFull, q, 0);
+        if (q >= n_rest) break;
+        const int ri = a.order[a.n_wide + q];
+        const ReadDesc& r = a.reads[ri];
+        if (!r.skip) {
+            if (r.ck)
+                fill_warp<kScores, true>(a, r, sm.warp_rings[warp], lane, forward_span(a, r));
+            else
+                fill_warp<kScores, false>(a, r, sm.warp_rings[warp], lane, forward_span(a, r));
+        }
+        __syncwarp();
+        __threadfence_block();
+        post_read_warp(a, p, ri, sm.post[warp], sm.warp_rings[warp], lane);
+    }
+    cluster.sync();  // neither block leaves while the other may still write its shared memory
+}
+
 // ---------------------------------------------------------------- launches
 cudaError_t launch_plain(const LaunchArgs& la, int* launches) {
     const int n = la.core.n_reads;
@@ -1197,11 +1626,38 @@ int batched_blocks_per_sm(bool scores) {
     return c;
 }
 
+static int cl_max_dyn_smem_set() {
+    static int done = 0;
+    if (!done) {
+        cudaFuncSetAttribute(abea_batched_cl_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(BatchedClSmem));
+        cudaFuncSetAttribute(abea_batched_cl_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(BatchedClSmem));
+        done = 1;
+    }
+    return done;
+}
+
 cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
     const int n = la.core.n_reads;
     abea_pre_kernel<<<n, 128, 0, la.stream>>>(la.pre);
     cudaEventRecordWithFlags(la.ev_pre, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     const bool scores = la.core.scores != nullptr;
+    if (la.cluster) {
+        // one wide read per cluster of two blocks; an even grid of one block per SM
+        cl_max_dyn_smem_set();
+        const int want = 2 * la.core.n_wide + (n - la.core.n_wide + kBatchedWarps - 1) / kBatchedWarps;
+        const int grid = 2 * std::max(1, std::min(la.sm_count / 2, (want + 1) / 2));
+        const size_t smem = sizeof(BatchedClSmem);
+        if (scores)
+            abea_batched_cl_kernel<true><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
+        else
+            abea_batched_cl_kernel<false><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
+        cudaEventRecordWithFlags(la.ev_core, la.stream,
+                                 la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+        *launches = 2;
+        return cudaGetLastError();
+    }
     const int max_blocks = batched_blocks_per_sm(scores) * la.sm_count;
     const int want = la.core.n_wide + (n - la.core.n_wide + kBatchedWarps - 1) / kBatchedWarps;
     const int grid = std::max(1, std::min(max_blocks, want));
@@ -1327,7 +1783,7 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     noalloc_write_desc<<<1, 1, 0, st>>>(d_desc, desc);
     PreArgs pre{d_desc, 1, g, sequence, events, model, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col};
     CoreArgs core{d_desc, 1, g, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col, trace, nullptr, band_k0,
-                  counters, nullptr, nullptr, 0, nullptr, nullptr};
+                  counters, nullptr, nullptr, 0, nullptr, nullptr, 1ll << 22};
     PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, km_rsd, last_col, trace, band_k0, pairs, n_pairs, best, status};
     abea_pre_kernel<<<1, 128, 0, st>>>(pre);
     abea_core_warp_kernel<false><<<1, 32, 0, st>>>(core);

@@ -45,6 +45,7 @@ struct CoreArgs {
     int32_t n_wide;                // leading reads of `order` that run on the wide shape
     float* ck;                     // checkpoint records of checkpointed reads
     uint8_t* ck_scratch;           // recompute scratch: kCkBands bands of trace per checkpointed read
+    long long spin_limit;          // polls before a device-side wait gives up (counters[2] counts those)
 };
 
 struct PostArgs {
@@ -111,6 +112,7 @@ struct LaunchArgs {
     cudaEvent_t ev_pre;   // recorded after pre
     cudaEvent_t ev_core;  // recorded after core (batched: after the fused core+post)
     bool capturing;       // the launches are being captured into a CUDA graph
+    bool cluster;         // batched form on clusters of two blocks (the cluster-pair wide shape)
 };
 
 // Plain form: pre, core, post — one block per read each, as the reference.

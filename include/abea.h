@@ -104,10 +104,13 @@ typedef enum {
     ABEA_OPT_SPIN_LIMIT = 4,    /* upper bound on any device-side wait, in polling iterations */
     ABEA_OPT_VAR_AWARE = 5,     /* 1: emissions use level_stdv*var and level_log_stdv+log_var (the
                                    reference ignores var, GPU/align_cuda.cl:509); taken at batch creation */
-    ABEA_OPT_TRACE_BUDGET = 6   /* bytes of backpointers a read may keep in HBM (128 per band); a read
+    ABEA_OPT_TRACE_BUDGET = 6,  /* bytes of backpointers a read may keep in HBM (128 per band); a read
                                    needing more keeps band-score checkpoints every 256 bands (4 bytes per
                                    band) and its traceback recomputes the trace 256 bands at a time.
                                    0 (default) = keep every trace.  Taken at batch creation. */
+    ABEA_OPT_WIDE_CLUSTER = 7   /* BATCHED: 1 = the longest reads run on a cluster of two blocks (the
+                                   second SM computes the emissions ahead into the first one's shared
+                                   memory); 0 = one block per wide read */
 } abea_option_t;
 
 typedef struct abea_ctx abea_ctx_t;

@@ -222,3 +222,22 @@ def test_graph_recaptured_for_each_batch_layout(lib, oracle_mod):
         gp, gc = ctx.align_batch(batch)
         op, oc, _ = oracle_batch(oracle_mod, batch)
         assert_same_alignments(batch, gp, gc, op, oc)
+
+
+@pytest.mark.parametrize("workload", ["small", "f5c_batch", "uneven"])
+def test_cluster_pair_wide_shape_is_exact(lib, oracle_mod, workload):
+    """ABEA_OPT_WIDE_CLUSTER: wide reads on a cluster of two blocks (the second
+    SM computing the emissions into the first one's shared memory) give the
+    plain form's AlignedPairs; on the small workload every read takes that shape."""
+    from abea_gb300 import synth
+    batch = synth.make_batch(workload, seed=4)
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    ctx.set_option(abea.OPT_WIDE_CLUSTER, 1)
+    if workload == "small":
+        ctx.set_option(abea.OPT_LONG_READ_BANDS, 1)
+    gp, gc = ctx.align_batch(batch)
+    if workload == "small":
+        op, oc, _ = oracle_batch(oracle_mod, batch)
+    else:
+        op, oc = abea.Context(0, abea.MODE_PLAIN).align_batch(batch)
+    assert_same_alignments(batch, gp, gc, op, oc)
