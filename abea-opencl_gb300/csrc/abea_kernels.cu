@@ -53,6 +53,8 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_group1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ float sel4(const float (&v)[4], int j) {
     float r = v[0];
@@ -1164,10 +1166,11 @@ struct Walk {
 // the event unless L).  Cells go to out (capacity cap) or, with kSum, their
 // emissions into w.sum.  Every lane calls it; lane 0 walks.  Returns true once
 // the path has ended (k or e below 0); false when it left the segment.
-template <bool kSum>
-__device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_end, int band_lo, PostSmem& sm,
+template <bool kSum, int kRing>
+__device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_end, int band_lo, uint8_t* ring,
                              int lane, Walk& w, abea_aligned_pair_t* out, int cap, const PostArgs& a,
                              const ReadDesc& r) {
+    static_assert(kRing >= 4 && (kRing & (kRing - 1)) == 0, "ring of a power of two chunks, at least four");
     const int bands_pad = (bands_end + 3) & ~3;
     const int c_lo = band_lo / kPostChunkBands;
     auto stage = [&](int c) {  // chunk c = bands [16c, 16c + 16)
@@ -1175,32 +1178,34 @@ __device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_en
             const int lo_band = c * kPostChunkBands;
             const int bytes = min(kPostChunkBands, bands_pad - lo_band) * kSlots;
             const uint8_t* src = trace + (int64_t)(lo_band - trace_band0) * kSlots;
-            uint8_t* dst = sm.tr + (c & 3) * (kPostChunkBands * kSlots);
+            uint8_t* dst = ring + (c & (kRing - 1)) * (kPostChunkBands * kSlots);
             for (int off = lane * 16; off < bytes; off += 32 * 16) cp_async16(dst + off, src + off);
         }
         cp_async_commit();  // an empty group keeps the group count in step
     };
-    const uint8_t* tb = sm.tr;
+    const uint8_t* tb = ring;
     auto T = [&](int band, int k) -> uint32_t {  // 0, 1 or 2; the clamp keeps every step a move
-        const int rb = band & 63;
+        const int rb = band & (kRing * kPostChunkBands - 1);
         return min((uint32_t)tb[((rb >> 2) << 9) | ((k & 127) << 2) | (rb & 3)], 2u);
     };
     int k = __shfl_sync(kFull, w.k, 0), e = __shfl_sync(kFull, w.e, 0);
     int c = (e + k + 2) / kPostChunkBands;
-    stage(c);
-    stage(c - 1);
-    stage(c - 2);
+    // chunks c and c-1 resident while chunk c is walked, kRing - 2 more in flight
+#pragma unroll
+    for (int j = 0; j < kRing - 1; ++j) stage(c - j);
     bool ended = false, left_seg = false;
     for (; c >= c_lo && !ended && !left_seg; --c) {
-        cp_async_wait_group1();  // chunks c and c-1 have landed; c-2 may be in flight
+        cp_async_wait_group<kRing - 3>();  // chunks c and c-1 have landed
         __syncwarp();
-        stage(c - 3);  // into the ring slot of chunk c+1, already walked
-        if (lane == 0) {
+        stage(c - (kRing - 1));  // into the ring slot of chunk c+1, already walked
+        // Every lane walks the same path (warp-uniform branches: the walk in one
+        // divergent lane ran slower); lane 0 stores the pairs.
+        {
             const int lo = c * kPostChunkBands;
             auto emit = [&](int kk, int ee, uint32_t f) {
                 if (kSum)
                     w.sum = __dadd_rn(w.sum, (double)path_emission(a, r, kk, ee));
-                else if (w.n_out < cap)
+                else if (w.n_out < cap && lane == 0)
                     out[w.n_out] = abea_aligned_pair_t{kk, ee};
                 ++w.n_out;
                 w.last_k = kk;
@@ -1220,25 +1225,29 @@ __device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_en
                     left_seg = band < band_lo;
                     break;
                 }
-                // this cell (band >= 2) and its predecessors (bands >= lo - 2)
-                const uint32_t f0 = T(band, k), fu = T(band - 1, k);
-                const uint32_t fl = T(band - 1, k - 1), fd = T(band - 2, k - 1);
-                emit(k, e, f0);
-                const int k1 = k - (int)((f0 & 1u) ^ 1u), e1 = e - (int)((f0 >> 1) ^ 1u);
-                const uint32_t f1 = ((fd | (fu << 8) | (fl << 16)) >> (8 * f0)) & 0xffu;
-                k = k1;
-                e = e1;
-                // the second step's byte is resident unless the first left the segment
-                if ((k1 | e1) < 0 || e1 + k1 + 2 < band_lo) continue;
-                emit(k1, e1, f1);
-                k = k1 - (int)((f1 & 1u) ^ 1u);
-                e = e1 - (int)((f1 >> 1) ^ 1u);
+                // Up to three steps from one round of loads: the backpointers of every
+                // cell two moves can reach (band offset db <= 4, k-mer offset dk <= 2;
+                // bands >= lo - 4, resident) packed 2 bits each at position 3*db + dk.
+                // A move adds 7 (D: db+2, dk+1), 3 (U: db+1) or 4 (L: db+1, dk+1).
+                const uint32_t W = T(band, k) | (T(band - 1, k) << 6) | (T(band - 1, k - 1) << 8) |
+                                   (T(band - 2, k) << 12) | (T(band - 2, k - 1) << 14) |
+                                   (T(band - 2, k - 2) << 16) | (T(band - 3, k - 1) << 20) |
+                                   (T(band - 3, k - 2) << 22) | (T(band - 4, k - 2) << 28);
+                uint32_t pos2 = 0;  // 2 * position
+#pragma unroll
+                for (int st = 0; st < 3; ++st) {
+                    const uint32_t f = (W >> pos2) & 3u;
+                    emit(k, e, f);
+                    k -= (int)((f & 1u) ^ 1u);
+                    e -= (int)((f >> 1) ^ 1u);
+                    pos2 += (0x86eu >> (4 * f)) & 0xfu;
+                    // a step that ends the path or leaves the resident segment stops the round
+                    if ((k | e) < 0 || e + k + 2 < band_lo) break;
+                }
             }
             w.k = k;
             w.e = e;
         }
-        ended = __shfl_sync(kFull, (int)ended, 0) != 0;
-        left_seg = __shfl_sync(kFull, (int)left_seg, 0) != 0;
     }
     cp_async_wait_all();
     __syncwarp();
@@ -1262,7 +1271,9 @@ __device__ __forceinline__ void recompute_segment(const CoreArgs& ca, const Read
 }
 
 // One warp per read: best end, traceback, QC, reverse (GPU/align_cuda.cl:618-899).
-__device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, PostSmem& sm, Rings& rg, int lane) {
+// `ring`: kRing * 2 KB of shared memory (16-byte aligned) for the traceback's trace chunks.
+template <int kRing>
+__device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* ring, Rings& rg, int lane) {
     const ReadDesc r = a.reads[ri];
     if (r.skip) {
         if (lane == 0) {
@@ -1310,14 +1321,14 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, Po
         // A finite end: the path only visits computed cells.
         Walk w{n_kmers - 1, best_e, 0, 0, 0, n_kmers - 1, 0, 0.0};
         if (!r.ck) {
-            walk_segment<false>(trace, 0, n_bands, 0, sm, lane, w, out, cap, a, r);
+            walk_segment<false, kRing>(trace, 0, n_bands, 0, ring, lane, w, out, cap, a, r);
         } else {
             // the trace was not kept: recompute it kCkBands bands at a time from
             // the checkpoints, top segment first, and walk each
             for (int seg = (w.k + w.e + 2) / kCkBands; seg >= 0; --seg) {
                 recompute_segment(ca, r, rg, lane, seg);
-                if (walk_segment<false>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands), seg * kCkBands,
-                                        sm, lane, w, out, cap, a, r))
+                if (walk_segment<false, kRing>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands),
+                                               seg * kCkBands, ring, lane, w, out, cap, a, r))
                     break;
             }
         }
@@ -1414,8 +1425,8 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, Po
             Walk w{n_kmers - 1, best_e, 0, 0, 0, n_kmers - 1, 0, 0.0};
             for (int seg = (w.k + w.e + 2) / kCkBands; seg >= 0; --seg) {
                 recompute_segment(ca, r, rg, lane, seg);
-                if (walk_segment<true>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands), seg * kCkBands,
-                                       sm, lane, w, out, cap, a, r))
+                if (walk_segment<true, kRing>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands),
+                                              seg * kCkBands, ring, lane, w, out, cap, a, r))
                     break;
             }
             sum = __shfl_sync(kFull, w.sum, 0);
@@ -1468,12 +1479,14 @@ __global__ void __launch_bounds__(32) abea_core_warp_kernel(CoreArgs a) {
         fill_warp<kScores, false>(a, r, rg, threadIdx.x, forward_span(a, r));
 }
 
+constexpr int kPostRingDeep = 8;  // trace chunks of a traceback with shared memory to spare (16 KB)
+
 __global__ void __launch_bounds__(32) abea_post_kernel(CoreArgs ca, PostArgs a) {
-    __shared__ __align__(16) PostSmem sm;
+    __shared__ __align__(16) uint8_t ring[kPostRingDeep * kPostChunkBands * kSlots];
     __shared__ __align__(16) Rings rg;  // recompute of checkpointed reads
     const int i = blockIdx.x;
     if (i >= a.n_reads) return;
-    post_read_warp(ca, a, i, sm, rg, threadIdx.x);
+    post_read_warp<kPostRingDeep>(ca, a, i, ring, rg, threadIdx.x);
 }
 
 // ---------------------------------------------------------------- batched form
@@ -1489,6 +1502,8 @@ static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSme
                   sizeof(Rings) % 16 == 0 && sizeof(PostSmem) % 16 == 0,
               "cp.async destinations must be 16-byte aligned");
 static_assert(sizeof(BatchedSmem) <= 227 * 1024, "batched kernel shared memory exceeds the per-block limit");
+static_assert(sizeof(WideSmem) >= kPostRingDeep * kPostChunkBands * kSlots && alignof(WideSmem) >= 16,
+              "the wide read's traceback ring lives in the wide fill's shared memory");
 
 
 template <bool kScores>
@@ -1508,7 +1523,10 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         if (!r.skip) fill_wide<kScores>(a, r, sm.wide, t);
         __syncthreads();
         __threadfence_block();
-        if (warp == 0) post_read_warp(a, p, wide_read, sm.post[0], sm.warp_rings[0], lane);
+        // the wide fill's shared memory is free: a deeper trace ring for the traceback
+        if (warp == 0)
+            post_read_warp<kPostRingDeep>(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0],
+                                          lane);
     }
     // phase 2: every warp pulls reads longest-first
     const int n_rest = a.n_reads - a.n_wide;
@@ -1527,7 +1545,7 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         }
         __syncwarp();
         __threadfence_block();
-        post_read_warp(a, p, ri, sm.post[warp], sm.warp_rings[warp], lane);
+        post_read_warp<4>(a, p, ri, sm.post[warp].tr, sm.warp_rings[warp], lane);
     }
 }
 
@@ -1570,7 +1588,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWideThreads, 1)
         // block reuses the fill's shared memory
         cluster.sync();
         __threadfence_block();
-        if (rank == 0 && warp == 0) post_read_warp(a, p, wide_read, sm.post[0], sm.warp_rings[0], lane);
+        if (rank == 0 && warp == 0) post_read_warp<4>(a, p, wide_read, sm.post[0].tr, sm.warp_rings[0], lane);
     }
     // phase 2: every warp pulls reads longest-first
     const int n_rest = a.n_reads - a.n_wide;
@@ -1589,7 +1607,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kWideThreads, 1)
         }
         __syncwarp();
         __threadfence_block();
-        post_read_warp(a, p, ri, sm.post[warp], sm.warp_rings[warp], lane);
+        post_read_warp<4>(a, p, ri, sm.post[warp].tr, sm.warp_rings[warp], lane);
     }
     cluster.sync();  // neither block leaves while the other may still write its shared memory
 }
