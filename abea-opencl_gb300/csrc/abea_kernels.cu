@@ -1166,10 +1166,16 @@ struct Walk {
 // the event unless L).  Cells go to out (capacity cap) or, with kSum, their
 // emissions into w.sum.  Every lane calls it; lane 0 walks.  Returns true once
 // the path has ended (k or e below 0); false when it left the segment.
-template <bool kSum, int kRing>
+// What a walk does with each cell: store the pair, sum its emission (walk
+// order), or record it in a speculative segment map (spec[band - band_lo] =
+// k | index << 22 for the cells below band spec_hi).
+enum WalkMode { kWalkPairs = 0, kWalkSum = 1, kWalkSpec = 2 };
+
+template <int kMode, int kRing>
 __device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_end, int band_lo, uint8_t* ring,
                              int lane, Walk& w, abea_aligned_pair_t* out, int cap, const PostArgs& a,
-                             const ReadDesc& r) {
+                             const ReadDesc& r, int32_t* spec = nullptr, int spec_hi = 0) {
+    constexpr bool kSum = kMode == kWalkSum;
     static_assert(kRing >= 4 && (kRing & (kRing - 1)) == 0, "ring of a power of two chunks, at least four");
     const int bands_pad = (bands_end + 3) & ~3;
     const int c_lo = band_lo / kPostChunkBands;
@@ -1203,6 +1209,14 @@ __device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_en
         {
             const int lo = c * kPostChunkBands;
             auto emit = [&](int kk, int ee, uint32_t f) {
+                if (kMode == kWalkSpec) {
+                    const int band = ee + kk + 2;
+                    if (band < spec_hi) {
+                        if (lane == 0) spec[band - band_lo] = kk | (w.n_out << 22);
+                        ++w.n_out;
+                    }
+                    return;
+                }
                 if (kSum)
                     w.sum = __dadd_rn(w.sum, (double)path_emission(a, r, kk, ee));
                 else if (w.n_out < cap && lane == 0)
@@ -1271,23 +1285,13 @@ __device__ __forceinline__ void recompute_segment(const CoreArgs& ca, const Read
 }
 
 // One warp per read: best end, traceback, QC, reverse (GPU/align_cuda.cl:618-899).
-// `ring`: kRing * 2 KB of shared memory (16-byte aligned) for the traceback's trace chunks.
-template <int kRing>
-__device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* ring, Rings& rg, int lane) {
-    const ReadDesc r = a.reads[ri];
-    if (r.skip) {
-        if (lane == 0) {
-            a.n_pairs[ri] = 0;
-            a.best_scores[ri] = -INFINITY;
-            a.status[ri] = 0;
-        }
-        return;
-    }
-    const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
+// Best end (GPU/align_cuda.cl:722-746): the first strict maximum of
+// s(e) = (float)(band + (n_events-e)*lp_trim) on the last k-mer column; the
+// whole warp calls it and every lane gets the result (best_e = 0 when no end is finite).
+__device__ void best_end_warp(const PostArgs& a, const ReadDesc& r, int lane, float& best_out, int& best_e_out) {
+    const int n_events = r.n_events;
     const double lp_trim = a.g.lp_trim;
     const float* lastc = a.last_col + r.ev_off;
-
-    // ---- best end: first strict maximum of s(e) = (float)(band + (n_events-e)*lp_trim)
     float best = -INFINITY;
     int best_e = 0x7fffffff;
     for (int e = lane; e < n_events; e += 32) {
@@ -1309,6 +1313,33 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, ui
         }
     }
     if (!(best > -INFINITY)) best_e = 0;
+    best_out = best;
+    best_e_out = best_e;
+}
+
+
+// QC, reverse and the per-read results of a walked path (GPU/align_cuda.cl:830-897).
+template <int kRing>
+__device__ void post_tail(const CoreArgs& ca, const PostArgs& a, int ri, const ReadDesc& r, uint8_t* ring, Rings& rg,
+                          int lane, float best, int best_e, int n_out, int max_gap, int status, int last_k,
+                          int last_from);
+
+// `ring`: kRing * 2 KB of shared memory (16-byte aligned) for the traceback's trace chunks.
+template <int kRing>
+__device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* ring, Rings& rg, int lane) {
+    const ReadDesc r = a.reads[ri];
+    if (r.skip) {
+        if (lane == 0) {
+            a.n_pairs[ri] = 0;
+            a.best_scores[ri] = -INFINITY;
+            a.status[ri] = 0;
+        }
+        return;
+    }
+    const int n_kmers = r.n_kmers, n_bands = r.n_bands;
+    float best;
+    int best_e;
+    best_end_warp(a, r, lane, best, best_e);
 
     abea_aligned_pair_t* out = a.pairs + r.out_off;
     const uint8_t* trace = a.trace + r.trace_off * kSlots;
@@ -1321,13 +1352,13 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, ui
         // A finite end: the path only visits computed cells.
         Walk w{n_kmers - 1, best_e, 0, 0, 0, n_kmers - 1, 0, 0.0};
         if (!r.ck) {
-            walk_segment<false, kRing>(trace, 0, n_bands, 0, ring, lane, w, out, cap, a, r);
+            walk_segment<kWalkPairs, kRing>(trace, 0, n_bands, 0, ring, lane, w, out, cap, a, r);
         } else {
             // the trace was not kept: recompute it kCkBands bands at a time from
             // the checkpoints, top segment first, and walk each
             for (int seg = (w.k + w.e + 2) / kCkBands; seg >= 0; --seg) {
                 recompute_segment(ca, r, rg, lane, seg);
-                if (walk_segment<false, kRing>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands),
+                if (walk_segment<kWalkPairs, kRing>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands),
                                                seg * kCkBands, ring, lane, w, out, cap, a, r))
                     break;
             }
@@ -1369,7 +1400,19 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, ui
     last_from = __shfl_sync(kFull, last_from, 0);
     __syncwarp();
     __threadfence_block();
+    post_tail<kRing>(ca, a, ri, r, ring, rg, lane, best, best_e, n_out, max_gap, status, last_k, last_from);
+}
 
+template <int kRing>
+__device__ void post_tail(const CoreArgs& ca, const PostArgs& a, int ri, const ReadDesc& r, uint8_t* ring, Rings& rg,
+                          int lane, float best, int best_e, int n_out, int max_gap, int status, int last_k,
+                          int last_from) {
+    const int n_kmers = r.n_kmers, n_bands = r.n_bands;
+    abea_aligned_pair_t* out = a.pairs + r.out_off;
+    const uint8_t* trace = a.trace + r.trace_off * kSlots;
+    const uint8_t* ck_seg = ca.ck_scratch + (int64_t)r.ck_slot * (kCkBands * kSlots);
+    const int32_t* bk0 = a.band_k0 + r.band_off;
+    const int cap = r.out_cap;
     int result = 0;
     bool reversed = false;
     if (status == 0 && n_out > 0) {
@@ -1425,7 +1468,7 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, ui
             Walk w{n_kmers - 1, best_e, 0, 0, 0, n_kmers - 1, 0, 0.0};
             for (int seg = (w.k + w.e + 2) / kCkBands; seg >= 0; --seg) {
                 recompute_segment(ca, r, rg, lane, seg);
-                if (walk_segment<true, kRing>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands),
+                if (walk_segment<kWalkSum, kRing>(ck_seg, seg * kCkBands, min((seg + 1) * kCkBands, n_bands),
                                               seg * kCkBands, ring, lane, w, out, cap, a, r))
                     break;
             }
@@ -1465,6 +1508,227 @@ __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, ui
     }
 }
 
+// ---------------------------------------------------------------- wide read's traceback, block-parallel
+// The wide read's traceback is on the batch's critical path while the rest of its
+// block waits, so the whole block walks it.  The path is cut into segments of
+// kSpecBands bands; each warp walks one segment of a window of kSpecWarps
+// segments speculatively, from the middle of the band kSpecMargin bands above
+// it (paths from different cells of a band merge within a few dozen bands),
+// recording its cells; warp 0 then walks the true path through the window and,
+// at the first cell it shares with a segment's speculative path, takes the rest
+// of that segment from the recording (the backpointers after a shared cell are
+// the same), and the warps copy those cells into the output in parallel.  A
+// segment whose speculative path the true one never meets is walked cell by
+// cell, so the result never depends on the speculation.  Gaps, the last cell
+// and the QC follow from the written pairs.
+constexpr int kPostRingDeep = 8;  // trace chunks of a traceback with shared memory to spare (16 KB)
+constexpr int kSpecBands = 256;
+constexpr int kSpecMargin = 64;
+constexpr int kSpecWarps = kWideThreads / 32;
+
+struct WidePostSmem {  // overlays the wide fill's shared memory once the fill is done
+    int32_t exit_k[kSpecWarps], exit_e[kSpecWarps], count[kSpecWarps], ended[kSpecWarps];
+    int32_t task_idx[kSpecWarps], task_off[kSpecWarps];
+    float best;
+    int32_t best_e, k, e, n_out, done, max_gap, last_from;
+    int32_t run[kWideThreads][4];  // per thread: leading L run, trailing L run, longest run, all L
+};
+
+// All kWideThreads threads of the block call it.  `spec_mem`: kSpecWarps *
+// kSpecBands int32 of shared memory; `rings`: one kRing-chunk trace ring per warp.
+template <int kRing>
+__device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* wide_mem, int32_t* spec_mem,
+                                PostSmem* rings, Rings& rg0, int t) {
+    const int warp = t >> 5, lane = t & 31;
+    WidePostSmem& ps = *reinterpret_cast<WidePostSmem*>(wide_mem);
+    const ReadDesc r = a.reads[ri];
+    // a path of several segments whose trace was kept and whose k-mers fit the map's 22 bits
+    if (r.skip || r.ck || r.n_kmers >= (1 << 22) || r.n_bands < 2 * kSpecBands) {
+        if (warp == 0) post_read_warp<kPostRingDeep>(ca, a, ri, wide_mem, rg0, lane);
+        return;
+    }
+    if (warp == 0) {
+        float b;
+        int be;
+        best_end_warp(a, r, lane, b, be);
+        if (lane == 0) {
+            ps.best = b;
+            ps.best_e = be;
+        }
+    }
+    __syncthreads();
+    const float best = ps.best;
+    const int best_e = ps.best_e;
+    __syncthreads();  // read before warp 0 may reuse the memory below
+    if (!(best > -INFINITY)) {
+        if (warp == 0) post_read_warp<kPostRingDeep>(ca, a, ri, wide_mem, rg0, lane);
+        return;
+    }
+    const int n_kmers = r.n_kmers, n_events = r.n_events, n_bands = r.n_bands, cap = r.out_cap;
+    const uint8_t* trace = a.trace + r.trace_off * kSlots;
+    const int32_t* bk0 = a.band_k0 + r.band_off;
+    abea_aligned_pair_t* out = a.pairs + r.out_off;
+    const int b0 = best_e + n_kmers - 1 + 2;  // band of the path's first cell
+    const int jtop = b0 / kSpecBands;
+    if (t == 0) {
+        ps.k = n_kmers - 1;
+        ps.e = best_e;
+        ps.n_out = 0;
+        ps.done = 0;
+    }
+    __syncthreads();
+    for (int jw = jtop; jw >= 0; jw -= kSpecWarps) {
+        // ---- speculative walks: warp w takes segment jw - w
+        {
+            const int j = jw - warp;
+            int32_t* spec = spec_mem + warp * kSpecBands;
+            for (int i = lane; i < kSpecBands; i += 32) spec[i] = -1;
+            __syncwarp();
+            if (j >= 0) {
+                const int seg_lo = j * kSpecBands, seg_hi = min(seg_lo + kSpecBands, n_bands);
+                int sk = n_kmers - 1, se = best_e;  // the top segment starts at the true start
+                if (j != jtop) {
+                    const int sb = min(seg_hi - 1 + kSpecMargin, b0);
+                    int kk = bk0[sb] + kBand / 2;  // the middle of band sb, moved inside the read
+                    kk = max(kk, max(0, sb - 2 - (n_events - 1)));
+                    kk = min(kk, min(n_kmers - 1, sb - 2));
+                    sk = kk;
+                    se = sb - 2 - kk;
+                }
+                Walk w{sk, se, 0, 0, 0, 0, 0, 0.0};
+                const bool ended = walk_segment<kWalkSpec, kRing>(trace, 0, n_bands, seg_lo, rings[warp].tr, lane, w,
+                                                                  nullptr, 0, a, r, spec, seg_hi);
+                if (lane == 0) {
+                    ps.exit_k[warp] = w.k;
+                    ps.exit_e[warp] = w.e;
+                    ps.count[warp] = w.n_out;
+                    ps.ended[warp] = ended ? 1 : 0;
+                }
+            }
+            if (lane == 0) ps.task_idx[warp] = -1;
+        }
+        __syncthreads();
+        // ---- the true path through the window (warp 0, every lane alike)
+        if (warp == 0) {
+            int k = ps.k, e = ps.e, n_out = ps.n_out;
+            bool done = ps.done != 0;
+            for (int wi = 0; wi < kSpecWarps && !done && jw - wi >= 0; ++wi) {
+                const int seg_lo = (jw - wi) * kSpecBands;
+                const int32_t* spec = spec_mem + wi * kSpecBands;
+                while (true) {
+                    if ((k | e) < 0) {
+                        done = true;
+                        break;
+                    }
+                    const int band = e + k + 2;
+                    if (band < seg_lo) break;
+                    const int sp = spec[band - seg_lo];
+                    if (sp >= 0 && (sp & 0x3fffff) == k) {
+                        // shared cell: the rest of the segment is the recorded path
+                        const int idx = sp >> 22;
+                        if (lane == 0) {
+                            ps.task_idx[wi] = idx;
+                            ps.task_off[wi] = n_out;
+                        }
+                        n_out += ps.count[wi] - idx;
+                        k = ps.exit_k[wi];
+                        e = ps.exit_e[wi];
+                        done = ps.ended[wi] != 0;
+                        break;
+                    }
+                    const uint32_t f = min((uint32_t)trace[trace_index(band, k & 127)], 2u);
+                    if (lane == 0 && n_out < cap) out[n_out] = abea_aligned_pair_t{k, e};
+                    ++n_out;
+                    k -= (int)((f & 1u) ^ 1u);
+                    e -= (int)((f >> 1) ^ 1u);
+                }
+            }
+            if (lane == 0) {
+                ps.k = k;
+                ps.e = e;
+                ps.n_out = n_out;
+                ps.done = done ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        // ---- the recorded parts, copied by their warps
+        {
+            const int j = jw - warp, idx0 = ps.task_idx[warp];
+            if (j >= 0 && idx0 >= 0) {
+                const int seg_lo = j * kSpecBands, off = ps.task_off[warp];
+                const int32_t* spec = spec_mem + warp * kSpecBands;
+                for (int i = lane; i < kSpecBands; i += 32) {
+                    const int sp = spec[i];
+                    if (sp < 0 || (sp >> 22) < idx0) continue;
+                    const int pos = off + (sp >> 22) - idx0, kk = sp & 0x3fffff;
+                    if (pos < cap) out[pos] = abea_aligned_pair_t{kk, seg_lo + i - 2 - kk};
+                }
+            }
+        }
+        __syncthreads();
+        if (ps.done) break;
+    }
+    const int n_out = ps.n_out;
+    __syncthreads();  // read before warp 0 may reuse the memory below
+    if (n_out > cap) {
+        // the path outgrew its output slot: the serial walk handles what the reference does
+        if (warp == 0) post_read_warp<kPostRingDeep>(ca, a, ri, wide_mem, rg0, lane);
+        return;
+    }
+    // ---- gaps: the move out of pair i is L iff pair i+1 is the k-mer before at the same event;
+    // out of the last pair, its backpointer
+    if (t == 0) {
+        const abea_aligned_pair_t lp = out[n_out - 1];
+        ps.last_from = (int)min((uint32_t)trace[trace_index(lp.read_pos + lp.ref_pos + 2, lp.ref_pos & 127)], 2u);
+    }
+    __syncthreads();
+    {
+        const int per = (n_out + kWideThreads - 1) / kWideThreads;
+        const int i0 = min(t * per, n_out), i1 = min(i0 + per, n_out);
+        int pre = 0, cur = 0, mx = 0;
+        bool all = true;
+        abea_aligned_pair_t p = i0 < i1 ? out[i0] : abea_aligned_pair_t{0, 0};
+        for (int i = i0; i < i1; ++i) {
+            bool is_l;
+            if (i + 1 < n_out) {
+                const abea_aligned_pair_t q = out[i + 1];
+                is_l = q.read_pos == p.read_pos && q.ref_pos == p.ref_pos - 1;
+                p = q;
+            } else {
+                is_l = ps.last_from == ABEA_FROM_L;
+            }
+            cur = is_l ? cur + 1 : 0;
+            mx = max(mx, cur);
+            if (all && is_l) ++pre;
+            all = all && is_l;
+        }
+        ps.run[t][0] = pre;
+        ps.run[t][1] = cur;
+        ps.run[t][2] = mx;
+        ps.run[t][3] = all ? 1 : 0;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    if (lane == 0) {
+        int carry = 0, best_run = 0;
+        for (int i = 0; i < kWideThreads; ++i) {
+            if (ps.run[i][3]) {
+                carry += ps.run[i][0];
+            } else {
+                best_run = max(best_run, carry + ps.run[i][0]);
+                carry = ps.run[i][1];
+            }
+            best_run = max(best_run, max(carry, ps.run[i][2]));
+        }
+        ps.max_gap = best_run;
+    }
+    __syncwarp();
+    const int max_gap = ps.max_gap, last_from = ps.last_from;
+    const int last_k = out[n_out - 1].ref_pos;
+    __syncwarp();
+    post_tail<kPostRingDeep>(ca, a, ri, r, wide_mem, rg0, lane, best, best_e, n_out, max_gap, 0, last_k, last_from);
+}
+
 // ---------------------------------------------------------------- plain form kernels
 template <bool kScores>
 __global__ void __launch_bounds__(32) abea_core_warp_kernel(CoreArgs a) {
@@ -1478,8 +1742,6 @@ __global__ void __launch_bounds__(32) abea_core_warp_kernel(CoreArgs a) {
     else
         fill_warp<kScores, false>(a, r, rg, threadIdx.x, forward_span(a, r));
 }
-
-constexpr int kPostRingDeep = 8;  // trace chunks of a traceback with shared memory to spare (16 KB)
 
 __global__ void __launch_bounds__(32) abea_post_kernel(CoreArgs ca, PostArgs a) {
     __shared__ __align__(16) uint8_t ring[kPostRingDeep * kPostChunkBands * kSlots];
@@ -1504,6 +1766,9 @@ static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSme
 static_assert(sizeof(BatchedSmem) <= 227 * 1024, "batched kernel shared memory exceeds the per-block limit");
 static_assert(sizeof(WideSmem) >= kPostRingDeep * kPostChunkBands * kSlots && alignof(WideSmem) >= 16,
               "the wide read's traceback ring lives in the wide fill's shared memory");
+static_assert(sizeof(WidePostSmem) <= sizeof(WideSmem), "the wide read's traceback state fits the fill's memory");
+static_assert(sizeof(Rings) * kBatchedWarps >= sizeof(int32_t) * kSpecWarps * kSpecBands,
+              "the speculative segment maps fit the warps' rings");
 
 
 template <bool kScores>
@@ -1523,10 +1788,9 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         if (!r.skip) fill_wide<kScores>(a, r, sm.wide, t);
         __syncthreads();
         __threadfence_block();
-        // the wide fill's shared memory is free: a deeper trace ring for the traceback
-        if (warp == 0)
-            post_read_warp<kPostRingDeep>(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0],
-                                          lane);
+        // the whole block walks the wide read's traceback (the fill's shared memory is free)
+        post_wide_block<4>(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide),
+                           reinterpret_cast<int32_t*>(sm.warp_rings), sm.post, sm.warp_rings[0], t);
     }
     // phase 2: every warp pulls reads longest-first
     const int n_rest = a.n_reads - a.n_wide;
