@@ -542,8 +542,23 @@ static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, boo
         else
             rest.push_back(i);
     }
+    // The warps of a block reaching the queue pick consecutive entries within
+    // microseconds, so longest-first order would put the 16 longest warp-shape reads
+    // on one SM, each slowed by the other fifteen.  The first wave (one read per
+    // warp of the grid) is the longest-first list read column by column over rows
+    // of kWarpsPerBlock, so that a block's burst of picks takes one read of each
+    // length rank; later picks stay longest-first.
+    constexpr int kWarpsPerBlock = 16;
+    const size_t nr = rest.size();
+    const size_t wave = std::min(nr, (size_t)blocks * kWarpsPerBlock);
+    const size_t rows = (wave + kWarpsPerBlock - 1) / kWarpsPerBlock;
     b->dev_order = wide;
-    b->dev_order.insert(b->dev_order.end(), rest.begin(), rest.end());
+    b->dev_order.reserve(wide.size() + nr);
+    for (size_t q = 0; q < rows * kWarpsPerBlock; ++q) {
+        const size_t i = (q % kWarpsPerBlock) * rows + q / kWarpsPerBlock;
+        if (i < wave) b->dev_order.push_back(rest[i]);
+    }
+    b->dev_order.insert(b->dev_order.end(), rest.begin() + (ptrdiff_t)wave, rest.end());
     return (int)wide.size();
 }
 
