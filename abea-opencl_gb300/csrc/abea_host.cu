@@ -524,16 +524,22 @@ static int64_t d2h_bytes(const abea_batch* b) {
     return (int64_t)sizeof(abea_aligned_pair_t) * b->pair_cap + (int64_t)sizeof(int32_t) * b->n_reads;
 }
 
-// Reads of the batched form that run on the wide shape: the longest reads whose
-// band count exceeds what one warp would carry if the whole batch were spread
-// evenly over the resident warps (their warp-shape fill would outlast the rest
-// of the batch), at most one per resident block, never a checkpointed read.
-// Fills b->dev_order with those reads first, then the rest longest first.
+// Reads of the batched form that run on the wide shape: the longest reads over
+// the threshold (the option, the autotuned value, or the heuristic below), at most
+// one per resident block, never a checkpointed read.  Fills b->dev_order with
+// those reads first, then the rest longest first.
 static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, bool scores, bool cluster) {
     const int blocks = cluster ? sm_count / 2 : batched_blocks_per_sm(scores) * sm_count;
-    int64_t total = 0;
-    for (const ReadDesc& r : b->reads) total += r.n_bands;
-    if (threshold <= 0) threshold = std::max<int64_t>(1, total / std::max(1, blocks * 8));
+    int64_t total = 0, longest = 0;
+    for (const ReadDesc& r : b->reads) {
+        total += r.n_bands;
+        longest = std::max<int64_t>(longest, r.n_bands);
+    }
+    // heuristic: a read wider than a warp's even share of the batch, and at least
+    // 30% of the longest read (a warp-shape read shares its SM with 15 others and
+    // runs at ~2,000-3,000 cycles per band, the wide shape at ~510 for one read)
+    if (threshold <= 0)
+        threshold = std::max<int64_t>({1, total / std::max(1, blocks * 8), longest * 3 / 10});
     std::vector<int32_t> wide, rest;
     for (int32_t i : b->order) {
         const ReadDesc& r = b->reads[(size_t)i];
@@ -542,23 +548,8 @@ static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, boo
         else
             rest.push_back(i);
     }
-    // The warps of a block reaching the queue pick consecutive entries within
-    // microseconds, so longest-first order would put the 16 longest warp-shape reads
-    // on one SM, each slowed by the other fifteen.  The first wave (one read per
-    // warp of the grid) is the longest-first list read column by column over rows
-    // of kWarpsPerBlock, so that a block's burst of picks takes one read of each
-    // length rank; later picks stay longest-first.
-    constexpr int kWarpsPerBlock = 16;
-    const size_t nr = rest.size();
-    const size_t wave = std::min(nr, (size_t)blocks * kWarpsPerBlock);
-    const size_t rows = (wave + kWarpsPerBlock - 1) / kWarpsPerBlock;
     b->dev_order = wide;
-    b->dev_order.reserve(wide.size() + nr);
-    for (size_t q = 0; q < rows * kWarpsPerBlock; ++q) {
-        const size_t i = (q % kWarpsPerBlock) * rows + q / kWarpsPerBlock;
-        if (i < wave) b->dev_order.push_back(rest[i]);
-    }
-    b->dev_order.insert(b->dev_order.end(), rest.begin() + (ptrdiff_t)wave, rest.end());
+    b->dev_order.insert(b->dev_order.end(), rest.begin(), rest.end());
     return (int)wide.size();
 }
 
@@ -682,8 +673,9 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
 }
 
 // Autotuner: times the batched form on `b` with candidate thresholds for the
-// wide shape — none, the heuristic, and the band counts of the reads ranked at
-// 1, 2, 3, 4, 6, 8, 12 and 16 sixteenths of the resident blocks — keeps the fastest for
+// wide shape — none, the heuristic, the band counts of the reads ranked at 1, 2,
+// 3, 4, 6, 8, 12 and 16 sixteenths of the resident blocks, and 15, 20, 45 and 60%
+// of the longest read — keeps the fastest for
 // this workload signature (longest read, read count and total bands, log2
 // buckets) and returns it.
 extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* best_threshold, float* best_ms) {
@@ -695,10 +687,16 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
     const int blocks = batched_blocks_per_sm(b->scores_kept) * c->sm_count;
     int64_t total = 0;
     for (const ReadDesc& r : b->reads) total += r.n_bands;
-    std::vector<int64_t> cands = {INT64_MAX, std::max<int64_t>(1, total / std::max(1, blocks * 8))};
+    int64_t longest = 0;
+    for (const ReadDesc& r : b->reads) longest = std::max<int64_t>(longest, r.n_bands);
+    std::vector<int64_t> cands = {INT64_MAX, std::max<int64_t>({1, total / std::max(1, blocks * 8), longest * 3 / 10})};
     for (int num : {1, 2, 3, 4, 6, 8, 12, 16}) {  // the longest num/16 of the resident blocks
         size_t k = std::min<size_t>(b->order.size(), (size_t)std::max(1, blocks * num / 16)) - 1;
         const int64_t c = std::max<int64_t>(1, b->reads[(size_t)b->order[k]].n_bands);
+        if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
+    }
+    for (int pct : {15, 20, 45, 60}) {  // fractions of the longest read
+        const int64_t c = std::max<int64_t>(1, longest * pct / 100);
         if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
     }
     int64_t best = 0;

@@ -1758,7 +1758,8 @@ struct BatchedSmem {
     WideSmem wide;                     // phase 1: the block's wide read
     Rings warp_rings[kBatchedWarps];   // phase 2: one per warp
     PostSmem post[kBatchedWarps];      // every warp's post staging
-    int32_t pick;
+    int32_t pick;                      // the block's wide read, or -1
+    int32_t free_rank;                 // rank among the blocks without a wide read, or -1
 };
 static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSmem, post) % 16 == 0 &&
                   sizeof(Rings) % 16 == 0 && sizeof(PostSmem) % 16 == 0,
@@ -1780,9 +1781,10 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
     if (t == 0) {
         const int q = atomicAdd(&a.queue[0], 1);
         sm.pick = q < a.n_wide ? a.order[q] : -1;
+        sm.free_rank = q < a.n_wide ? -1 : q - a.n_wide;
     }
     __syncthreads();
-    const int wide_read = sm.pick;
+    const int wide_read = sm.pick, free_rank = sm.free_rank;
     if (wide_read >= 0) {
         const ReadDesc& r = a.reads[wide_read];
         if (!r.skip) fill_wide<kScores>(a, r, sm.wide, t);
@@ -1792,13 +1794,25 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         post_wide_block<4>(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide),
                            reinterpret_cast<int32_t*>(sm.warp_rings), sm.post, sm.warp_rings[0], t);
     }
-    // phase 2: every warp pulls reads longest-first
+    // phase 2: the first wave is static, the blocks without a wide read taking the
+    // longest remaining reads round-robin (warp w of free block f: read f + F*w),
+    // so that the long ones spread over the SMs; then every warp pulls the rest
+    // longest-first
     const int n_rest = a.n_reads - a.n_wide;
-    while (true) {
-        int q = 0;
-        if (lane == 0) q = atomicAdd(&a.queue[1], 1);
-        q = __shfl_sync(kFull, q, 0);
-        if (q >= n_rest) break;
+    const int n_free = (int)gridDim.x - min(a.n_wide, (int)gridDim.x);
+    const int wave = min(n_rest, n_free * kBatchedWarps);
+    for (int pass = 0;; ++pass) {
+        int q;
+        if (pass == 0) {
+            if (free_rank < 0) continue;
+            q = free_rank + n_free * warp;
+            if (q >= wave) continue;
+        } else {
+            q = 0;
+            if (lane == 0) q = wave + atomicAdd(&a.queue[1], 1);
+            q = __shfl_sync(kFull, q, 0);
+            if (q >= n_rest) break;
+        }
         const int ri = a.order[a.n_wide + q];
         const ReadDesc& r = a.reads[ri];
         if (!r.skip) {
@@ -1940,9 +1954,9 @@ cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
         *launches = 2;
         return cudaGetLastError();
     }
+    // every resident block: the blocks without a wide read share the first wave
     const int max_blocks = batched_blocks_per_sm(scores) * la.sm_count;
-    const int want = la.core.n_wide + (n - la.core.n_wide + kBatchedWarps - 1) / kBatchedWarps;
-    const int grid = std::max(1, std::min(max_blocks, want));
+    const int grid = std::max(1, std::min(max_blocks, n));
     const size_t smem = sizeof(BatchedSmem);
     if (scores)
         abea_batched_kernel<true><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
