@@ -241,3 +241,30 @@ def test_cluster_pair_wide_shape_is_exact(lib, oracle_mod, workload):
     else:
         op, oc = abea.Context(0, abea.MODE_PLAIN).align_batch(batch)
     assert_same_alignments(batch, gp, gc, op, oc)
+
+
+@pytest.mark.parametrize("threshold", [1, 512])
+def test_wide_shape_block_traceback_on_the_edge_cases(lib, ref_synthetic, threshold):
+    """Reads of 512 bands or more on the wide shape have their traceback walked by
+    the whole block (speculative segments spliced into the true path).  The
+    reference fixture's long edge cases go through it: a path longer than its
+    output slot (few_events_400: the serial walk takes over), reads that fail the
+    QC, reads over several 256-band segments.  Shorter reads take the serial
+    walk on the wide shape when the threshold is one band."""
+    batch, names, counts, pairs, _ = ref_synthetic
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    ctx.set_option(abea.OPT_LONG_READ_BANDS, threshold)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    assert np.array_equal(gc, counts)
+    got = abea.split_pairs(batch, gp, gc)
+    for i, name in enumerate(names):
+        assert np.array_equal(got[i], pairs[i]), name
+    # the adjoint reads the path the traceback left
+    g = dev.backward()
+    g0 = abea.Context(0, abea.MODE_PLAIN).upload(batch)
+    g0.run()
+    h = g0.backward()
+    assert np.array_equal(g["path_emission"], h["path_emission"])
+    assert np.array_equal(g["status"], h["status"])
