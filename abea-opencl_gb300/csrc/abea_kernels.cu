@@ -1119,6 +1119,26 @@ __device__ __forceinline__ float path_emission(const PostArgs& a, const ReadDesc
     return emission_ieee(a.ev_mean[r.ev_off + e], a.km_gm[ko], a.km_sd[ko], a.km_k1[ko]);
 }
 
+// One pair's emission for the QC sum as an integer multiple of 2^-24 (exact when
+// 0.5 <= |em| < 2^20; `exact` turns false otherwise).  The division is Markstein's
+// (div_rn): no routine call, so that the loads of several cells are in flight at once.
+__device__ __forceinline__ void qc_term(const PostArgs& a, const ReadDesc& r, abea_aligned_pair_t p, long long& isum,
+                                        long long& iabs, bool& exact) {
+    const int64_t ko = r.km_off + p.ref_pos;
+    bool ok;
+    const float em =
+        emission_rn(a.ev_mean[r.ev_off + p.read_pos], a.km_gm[ko], a.km_sd[ko], a.km_rsd[ko], a.km_k1[ko], ok);
+    const float aem = fabsf(em);
+    const long long q = __float2ll_rn(__fmul_rn(em, 16777216.0f));
+    const bool in = ok && aem >= 0.5f && aem < 1048576.0f;
+    isum += in ? q : 0ll;
+    iabs += in ? (q < 0 ? -q : q) : 0ll;
+    exact = exact && in;
+}
+
+__device__ __forceinline__ void post_write(const PostArgs& a, int ri, int result, float best, int best_e, int status,
+                                           int n_out, int cap, bool reversed, int last_from);
+
 // One traceback step: D -> (k-1, e-1), U -> (k, e-1), L -> (k-1, e); gap counting.
 __device__ __forceinline__ void step_back(uint32_t from, int& k, int& e, int& gap, int& max_gap) {
     k -= (from != ABEA_FROM_U) ? 1 : 0;
@@ -1423,24 +1443,10 @@ __device__ void post_tail(const CoreArgs& ca, const PostArgs& a, int ri, const R
             // Every emission with 0.5 <= |em| < 2^20 is a multiple of 2^-24; when the
             // magnitudes sum below 2^53 * 2^-24 all of the reference's partial double
             // sums are exact and equal this integer sum, whatever the order.
-            // The division is Markstein's (div_rn): no routine call, so that the
-            // loads of four cells are in flight at once.
             long long isum = 0, iabs = 0;
             bool exact = true;
 #pragma unroll 4
-            for (int i2 = lane; i2 < n_out; i2 += 32) {
-                const abea_aligned_pair_t p = out[i2];
-                const int64_t ko = r.km_off + p.ref_pos;
-                bool ok;
-                const float em = emission_rn(a.ev_mean[r.ev_off + p.read_pos], a.km_gm[ko], a.km_sd[ko], a.km_rsd[ko],
-                                             a.km_k1[ko], ok);
-                const float aem = fabsf(em);
-                const long long q = __float2ll_rn(__fmul_rn(em, 16777216.0f));
-                const bool in = ok && aem >= 0.5f && aem < 1048576.0f;
-                isum += in ? q : 0ll;
-                iabs += in ? (q < 0 ? -q : q) : 0ll;
-                exact = exact && in;
-            }
+            for (int i2 = lane; i2 < n_out; i2 += 32) qc_term(a, r, out[i2], isum, iabs, exact);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
                 isum += __shfl_xor_sync(kFull, isum, off);
@@ -1492,7 +1498,14 @@ __device__ void post_tail(const CoreArgs& ca, const PostArgs& a, int ri, const R
     } else if (status != 0) {
         result = status;
     }
-    if (lane == 0) {
+    if (lane == 0) post_write(a, ri, result, best, best_e, status, n_out, cap, reversed, last_from);
+}
+
+// The per-read results, and the path the adjoint reads: its length, whether the
+// output holds it in walk order or reversed, and the move into its last walked cell.
+__device__ __forceinline__ void post_write(const PostArgs& a, int ri, int result, float best, int best_e, int status,
+                                           int n_out, int cap, bool reversed, int last_from) {
+    {
         a.n_pairs[ri] = result;
         a.best_scores[ri] = best;
         a.status[ri] = status;
@@ -1530,7 +1543,10 @@ struct WidePostSmem {  // overlays the wide fill's shared memory once the fill i
     int32_t exit_k[kSpecWarps], exit_e[kSpecWarps], count[kSpecWarps], ended[kSpecWarps];
     int32_t task_idx[kSpecWarps], task_off[kSpecWarps];
     float best;
-    int32_t best_e, k, e, n_out, done, max_gap, last_from;
+    int32_t best_e, k, e, n_out, done, max_gap, last_from, last_k, pass, qc_exact;
+    float wbest[kSpecWarps];
+    int32_t wbest_e[kSpecWarps], qexact[kSpecWarps];
+    long long qsum[kSpecWarps], qabs[kSpecWarps];
     int32_t run[kWideThreads][4];  // per thread: leading L run, trailing L run, longest run, all L
 };
 
@@ -1547,13 +1563,44 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
         if (warp == 0) post_read_warp<kPostRingDeep>(ca, a, ri, wide_mem, rg0, lane);
         return;
     }
-    if (warp == 0) {
-        float b;
-        int be;
-        best_end_warp(a, r, lane, b, be);
+    {
+        // best end by the block: the first strict maximum is the largest value at the
+        // smallest event among equals, per thread, per warp, then over the warps
+        const double lp_trim = a.g.lp_trim;
+        const float* lastc = a.last_col + r.ev_off;
+        float b = -INFINITY;
+        int be = 0x7fffffff;
+        for (int e = t; e < r.n_events; e += kWideThreads) {
+            const float v = lastc[e];
+            if (v == -INFINITY) continue;
+            const float sv = __double2float_rn(__dadd_rn((double)v, __dmul_rn((double)(r.n_events - e), lp_trim)));
+            if (sv > b) {
+                b = sv;
+                be = e;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ob = __shfl_xor_sync(kFull, b, off);
+            const int oe = __shfl_xor_sync(kFull, be, off);
+            if (ob > b || (ob == b && oe < be)) {
+                b = ob;
+                be = oe;
+            }
+        }
         if (lane == 0) {
+            ps.wbest[warp] = b;
+            ps.wbest_e[warp] = be;
+        }
+        __syncthreads();
+        if (t == 0) {
+            for (int w = 1; w < kSpecWarps; ++w)
+                if (ps.wbest[w] > b || (ps.wbest[w] == b && ps.wbest_e[w] < be)) {
+                    b = ps.wbest[w];
+                    be = ps.wbest_e[w];
+                }
             ps.best = b;
-            ps.best_e = be;
+            ps.best_e = b > -INFINITY ? be : 0;
         }
     }
     __syncthreads();
@@ -1707,9 +1754,26 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
         ps.run[t][2] = mx;
         ps.run[t][3] = all ? 1 : 0;
     }
+    // ---- QC (GPU/align_cuda.cl:856-882): the exact integer emission sum by the block
+    {
+        long long isum = 0, iabs = 0;
+        bool exact = true;
+#pragma unroll 4
+        for (int i = t; i < n_out; i += kWideThreads) qc_term(a, r, out[i], isum, iabs, exact);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            isum += __shfl_xor_sync(kFull, isum, off);
+            iabs += __shfl_xor_sync(kFull, iabs, off);
+        }
+        exact = __all_sync(kFull, exact);
+        if (lane == 0) {
+            ps.qsum[warp] = isum;
+            ps.qabs[warp] = iabs;
+            ps.qexact[warp] = exact ? 1 : 0;
+        }
+    }
     __syncthreads();
-    if (warp != 0) return;
-    if (lane == 0) {
+    if (t == 0) {
         int carry = 0, best_run = 0;
         for (int i = 0; i < kWideThreads; ++i) {
             if (ps.run[i][3]) {
@@ -1720,13 +1784,39 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
             }
             best_run = max(best_run, max(carry, ps.run[i][2]));
         }
+        long long isum = 0, iabs = 0;
+        bool exact = true;
+        for (int w = 0; w < kSpecWarps; ++w) {
+            isum += ps.qsum[w];
+            iabs += ps.qabs[w];
+            exact = exact && ps.qexact[w];
+        }
+        exact = exact && iabs < (1ll << 53);
+        const int last_k = out[n_out - 1].ref_pos;  // the last cell walked (before the reversal)
+        const double sum = __dmul_rn((double)isum, 5.9604644775390625e-08);  // * 2^-24
+        const double avg = __ddiv_rn(sum, (double)n_out);
         ps.max_gap = best_run;
+        ps.last_k = last_k;
+        ps.qc_exact = exact ? 1 : 0;
+        ps.pass = (!(avg < -5.0) && last_k == 0 && best_run <= 50) ? 1 : 0;
     }
-    __syncwarp();
-    const int max_gap = ps.max_gap, last_from = ps.last_from;
-    const int last_k = out[n_out - 1].ref_pos;
-    __syncwarp();
-    post_tail<kPostRingDeep>(ca, a, ri, r, wide_mem, rg0, lane, best, best_e, n_out, max_gap, 0, last_k, last_from);
+    __syncthreads();
+    const int max_gap = ps.max_gap, last_from = ps.last_from, last_k = ps.last_k;
+    if (!ps.qc_exact) {
+        // emissions outside the exact integer form: warp 0 sums serially in walk order
+        if (warp == 0)
+            post_tail<kPostRingDeep>(ca, a, ri, r, wide_mem, rg0, lane, best, best_e, n_out, max_gap, 0, last_k,
+                                     last_from);
+        return;
+    }
+    const bool pass = ps.pass != 0;
+    if (pass)  // reverse in place (GPU/align_cuda.cl:830-843)
+        for (int i = t; i < n_out / 2; i += kWideThreads) {
+            const abea_aligned_pair_t x = out[i], y = out[n_out - 1 - i];
+            out[i] = y;
+            out[n_out - 1 - i] = x;
+        }
+    if (t == 0) post_write(a, ri, pass ? n_out : 0, best, best_e, 0, n_out, cap, pass, last_from);
 }
 
 // ---------------------------------------------------------------- plain form kernels
