@@ -89,6 +89,7 @@ struct abea_batch {
     int64_t trace_pad_total = 0;  // bands of kept traces
     int64_t ck_floats = 0;        // checkpoint records
     int32_t n_ck = 0;             // checkpointed reads (recompute scratch slots)
+    int32_t n_spec = 0;           // block-parallel traceback scratch slots
     // device pointers (sub-ranges of the slab)
     DevSlab slab;
     ReadDesc* d_reads = nullptr;
@@ -101,6 +102,7 @@ struct abea_batch {
     float* d_scores = nullptr;
     float* d_ck = nullptr;           // checkpoint records
     uint8_t* d_ck_scratch = nullptr; // one kCkBands-band trace segment per checkpointed read
+    int32_t* d_spec = nullptr;       // cell maps of the wide reads' block-parallel tracebacks
     int32_t* d_band_k0 = nullptr;
     abea_aligned_pair_t* d_pairs = nullptr;
     int32_t* d_n_pairs = nullptr;
@@ -391,6 +393,10 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, in
     b->trace_pad_total = tbands;
     b->ck_floats = ckf;
     b->n_ck = n_ck;
+    int32_t n_spec = 0;
+    for (const ReadDesc& r : b->reads)
+        if (!r.skip && !r.ck && r.n_bands >= kSpecMinBands) ++n_spec;
+    b->n_spec = std::min(n_spec, kSpecMaxSlots);
     b->pair_cap = 2 * ev_end;
     b->band_cells = cells;
     // longest first; ties by index
@@ -407,7 +413,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Carves the device slab; grows it when needed.
 static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 0) {
     size_t n = (size_t)std::max(b->n_reads, 1);
-    size_t sizes[31] = {
+    size_t sizes[32] = {
         sizeof(ReadDesc) * n,                                   // reads
         (size_t)std::max<int64_t>(b->seq_bytes, 1),             // seq
         sizeof(abea_event_t) * (size_t)std::max<int64_t>(b->n_events_total, 1),
@@ -438,8 +444,9 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
         sizeof(double) * 2 * ABEA_NUM_KMER,  // grad_model
         sizeof(float) * (size_t)std::max<int64_t>(b->ck_floats, 16),  // checkpoints
         (size_t)kCkBands * kSlots * (size_t)std::max<int32_t>(b->n_ck, 0),  // recompute scratch
+        sizeof(int32_t) * kSpecRound * kSpecBands * (size_t)b->n_spec,      // traceback cell maps
         0};
-    const int n_bufs = 30;
+    const int n_bufs = 31;
     size_t total = 0;
     for (int i = 0; i < n_bufs; ++i) total += align256(sizes[i]);
     if (total > b->slab.bytes) {
@@ -456,7 +463,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
         b->slab.bytes = want;
     }
     char* p = (char*)b->slab.base;
-    void* ptrs[31];
+    void* ptrs[32];
     for (int i = 0; i < n_bufs; ++i) {
         ptrs[i] = sizes[i] ? (void*)p : nullptr;
         p += align256(sizes[i]);
@@ -491,6 +498,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
     b->d_grad_model = (double*)ptrs[27];
     b->d_ck = (float*)ptrs[28];
     b->d_ck_scratch = (uint8_t*)ptrs[29];
+    b->d_spec = (int32_t*)ptrs[30];
     b->scores_kept = scores;
     b->carve.assign(1, (uint64_t)(uintptr_t)b->slab.base);
     for (int i = 0; i < n_bufs; ++i) b->carve.push_back((uint64_t)sizes[i]);
@@ -561,7 +569,8 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
                      b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col};
     la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
                        b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
-                       b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch,
+                       b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch, b->d_spec,
+                       b->n_spec,
                        (long long)c->spin_limit};
     la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1, b->d_km_rsd,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
@@ -1194,6 +1203,11 @@ static int64_t slab_fixed_bytes() {
            32 * 256 + 16 * 1024;
 }
 
+// Traceback cell maps of a batch holding n reads of at least kSpecMinBands bands.
+static int64_t spec_bytes(int64_t n) {
+    return (int64_t)sizeof(int32_t) * kSpecRound * kSpecBands * std::min<int64_t>(n, kSpecMaxSlots);
+}
+
 static void CUDART_CB stamp_now(void* p) {
     *(std::chrono::steady_clock::time_point*)p = std::chrono::steady_clock::now();
 }
@@ -1244,22 +1258,27 @@ extern "C" abea_status_t abea_align_stream(abea_ctx_t* c, const abea_stream_conf
     const bool scores = c->store_scores != 0;
     std::vector<int32_t> cut = {0};
     std::vector<int64_t> cut_bytes;
-    int64_t acc = slab_fixed_bytes(), max_bytes = 0, cells = 0;
+    int64_t acc = slab_fixed_bytes(), max_bytes = 0, cells = 0, n_long = 0;
     for (int32_t i = 0; i < n_reads; ++i) {
         const int64_t rb = read_device_bytes(read_len[i], n_events[i], c->trace_budget, scores);
-        if (i > cut.back() && acc + rb > budget) {
+        const int64_t nk = (int64_t)read_len[i] - ABEA_KMER_SIZE + 1;
+        const int64_t nb = nk > 0 && n_events[i] > 0 ? n_events[i] + nk + 2 : 0;
+        const bool trace_kept = c->trace_budget <= 0 || round_up(nb, 4) * kSlots <= c->trace_budget;
+        const int64_t lg = nb >= kSpecMinBands && trace_kept ? 1 : 0;  // a traceback map slot
+        if (i > cut.back() && acc + rb + spec_bytes(n_long + lg) > budget) {
             cut.push_back(i);
-            cut_bytes.push_back(acc);
-            max_bytes = std::max(max_bytes, acc);
+            cut_bytes.push_back(acc + spec_bytes(n_long));
+            max_bytes = std::max(max_bytes, acc + spec_bytes(n_long));
             acc = slab_fixed_bytes();
+            n_long = 0;
         }
         acc += rb;
-        const int64_t nk = (int64_t)read_len[i] - ABEA_KMER_SIZE + 1;
-        if (nk > 0 && n_events[i] > 0) cells += (n_events[i] + nk + 2) * (int64_t)kBand;
+        n_long += lg;
+        cells += nb * (int64_t)kBand;
     }
     cut.push_back(n_reads);
-    cut_bytes.push_back(acc);
-    max_bytes = std::max(max_bytes, acc);
+    cut_bytes.push_back(acc + spec_bytes(n_long));
+    max_bytes = std::max(max_bytes, acc + spec_bytes(n_long));
     const int nb = (int)cut.size() - 1;
     // resources kept by the context
     if (!c->copy_stream) CUDA_TRY(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));

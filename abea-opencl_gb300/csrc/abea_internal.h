@@ -66,6 +66,15 @@ struct ReadDesc {
 constexpr int kCkBands = 256;
 constexpr int kCkStride = 264;  // 128 + 128 scores, k0, e0, padding to 16 bytes
 
+// Block-parallel traceback of a wide read: segments of kSpecBands bands, walked
+// speculatively kSpecRound at a time (one thread each), their cell maps in a
+// scratch slot of kSpecRound * kSpecBands int32 per wide read in flight.  Reads of
+// at least kSpecMinBands bands qualify; at most kSpecMaxSlots slots per batch.
+constexpr int kSpecBands = 256;
+constexpr int kSpecRound = 512;
+constexpr int kSpecMinBands = 2 * kSpecBands;
+constexpr int kSpecMaxSlots = 256;
+
 struct GlobalConsts {
     double lp_skip;  // log(1e-10)
     double lp_trim;  // log(0.01)

@@ -1524,42 +1524,42 @@ __device__ __forceinline__ void post_write(const PostArgs& a, int ri, int result
 // ---------------------------------------------------------------- wide read's traceback, block-parallel
 // The wide read's traceback is on the batch's critical path while the rest of its
 // block waits, so the whole block walks it.  The path is cut into segments of
-// kSpecBands bands; each warp walks one segment of a window of kSpecWarps
-// segments speculatively, from the middle of the band kSpecMargin bands above
-// it (paths from different cells of a band merge within a few dozen bands),
-// recording its cells; warp 0 then walks the true path through the window and,
-// at the first cell it shares with a segment's speculative path, takes the rest
-// of that segment from the recording (the backpointers after a shared cell are
-// the same), and the warps copy those cells into the output in parallel.  A
-// segment whose speculative path the true one never meets is walked cell by
-// cell, so the result never depends on the speculation.  Gaps, the last cell
-// and the QC follow from the written pairs.
-constexpr int kPostRingDeep = 8;  // trace chunks of a traceback with shared memory to spare (16 KB)
-constexpr int kSpecBands = 256;
+// kSpecBands bands.  Every thread walks one segment speculatively (up to
+// kSpecRound segments at once), from the middle of the band kSpecMargin bands
+// above it (paths from different cells of a band merge within a few dozen bands),
+// recording its cells in a map in global scratch (L2); warp 0 then walks the true
+// path through the round and, at the first cell it shares with a segment's
+// speculative path, takes the rest of that segment from the map (the
+// backpointers after a shared cell are the same); the block copies those cells
+// into the output.  A segment whose speculative path the true one never meets is
+// walked cell by cell, so the result never depends on the speculation.  Gaps, the
+// last cell and the QC follow from the written pairs.
 constexpr int kSpecMargin = 64;
 constexpr int kSpecWarps = kWideThreads / 32;
+constexpr int kPostRingDeep = 8;  // trace chunks of a traceback with shared memory to spare (16 KB)
 
 struct WidePostSmem {  // overlays the wide fill's shared memory once the fill is done
-    int32_t exit_k[kSpecWarps], exit_e[kSpecWarps], count[kSpecWarps], ended[kSpecWarps];
-    int32_t task_idx[kSpecWarps], task_off[kSpecWarps];
     float best;
-    int32_t best_e, k, e, n_out, done, max_gap, last_from, last_k, pass, qc_exact;
+    int32_t best_e, k, e, n_out, done, max_gap, last_from, last_k, pass, qc_exact, slot;
     float wbest[kSpecWarps];
     int32_t wbest_e[kSpecWarps], qexact[kSpecWarps];
     long long qsum[kSpecWarps], qabs[kSpecWarps];
-    int32_t run[kWideThreads][4];  // per thread: leading L run, trailing L run, longest run, all L
+    union {
+        struct {  // per segment of the round: where its speculative walk left, and the splice
+            int32_t exit_k[kSpecRound], exit_e[kSpecRound], count[kSpecRound], ended[kSpecRound];
+            int32_t task_idx[kSpecRound], task_off[kSpecRound];
+        } seg;
+        int32_t run[kWideThreads][4];  // per thread: leading L run, trailing L run, longest run, all L
+    };
 };
 
-// All kWideThreads threads of the block call it.  `spec_mem`: kSpecWarps *
-// kSpecBands int32 of shared memory; `rings`: one kRing-chunk trace ring per warp.
-template <int kRing>
-__device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* wide_mem, int32_t* spec_mem,
-                                PostSmem* rings, Rings& rg0, int t) {
+// All kWideThreads threads of the block call it.
+__device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* wide_mem, Rings& rg0, int t) {
     const int warp = t >> 5, lane = t & 31;
     WidePostSmem& ps = *reinterpret_cast<WidePostSmem*>(wide_mem);
     const ReadDesc r = a.reads[ri];
     // a path of several segments whose trace was kept and whose k-mers fit the map's 22 bits
-    if (r.skip || r.ck || r.n_kmers >= (1 << 22) || r.n_bands < 2 * kSpecBands) {
+    if (r.skip || r.ck || r.n_kmers >= (1 << 22) || r.n_bands < kSpecMinBands) {
         if (warp == 0) post_read_warp<kPostRingDeep>(ca, a, ri, wide_mem, rg0, lane);
         return;
     }
@@ -1601,13 +1601,14 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
                 }
             ps.best = b;
             ps.best_e = b > -INFINITY ? be : 0;
+            ps.slot = b > -INFINITY ? atomicAdd(&ca.queue[2], 1) : 0;  // a scratch slot for the maps
         }
     }
     __syncthreads();
     const float best = ps.best;
-    const int best_e = ps.best_e;
+    const int best_e = ps.best_e, slot = ps.slot;
     __syncthreads();  // read before warp 0 may reuse the memory below
-    if (!(best > -INFINITY)) {
+    if (!(best > -INFINITY) || slot >= ca.n_spec) {
         if (warp == 0) post_read_warp<kPostRingDeep>(ca, a, ri, wide_mem, rg0, lane);
         return;
     }
@@ -1615,6 +1616,7 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
     const uint8_t* trace = a.trace + r.trace_off * kSlots;
     const int32_t* bk0 = a.band_k0 + r.band_off;
     abea_aligned_pair_t* out = a.pairs + r.out_off;
+    int32_t* map = ca.spec + (int64_t)slot * (kSpecRound * kSpecBands);
     const int b0 = best_e + n_kmers - 1 + 2;  // band of the path's first cell
     const int jtop = b0 / kSpecBands;
     if (t == 0) {
@@ -1623,45 +1625,51 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
         ps.n_out = 0;
         ps.done = 0;
     }
-    __syncthreads();
-    for (int jw = jtop; jw >= 0; jw -= kSpecWarps) {
-        // ---- speculative walks: warp w takes segment jw - w
-        {
-            const int j = jw - warp;
-            int32_t* spec = spec_mem + warp * kSpecBands;
-            for (int i = lane; i < kSpecBands; i += 32) spec[i] = -1;
-            __syncwarp();
-            if (j >= 0) {
-                const int seg_lo = j * kSpecBands, seg_hi = min(seg_lo + kSpecBands, n_bands);
-                int sk = n_kmers - 1, se = best_e;  // the top segment starts at the true start
-                if (j != jtop) {
-                    const int sb = min(seg_hi - 1 + kSpecMargin, b0);
-                    int kk = bk0[sb] + kBand / 2;  // the middle of band sb, moved inside the read
-                    kk = max(kk, max(0, sb - 2 - (n_events - 1)));
-                    kk = min(kk, min(n_kmers - 1, sb - 2));
-                    sk = kk;
-                    se = sb - 2 - kk;
-                }
-                Walk w{sk, se, 0, 0, 0, 0, 0, 0.0};
-                const bool ended = walk_segment<kWalkSpec, kRing>(trace, 0, n_bands, seg_lo, rings[warp].tr, lane, w,
-                                                                  nullptr, 0, a, r, spec, seg_hi);
-                if (lane == 0) {
-                    ps.exit_k[warp] = w.k;
-                    ps.exit_e[warp] = w.e;
-                    ps.count[warp] = w.n_out;
-                    ps.ended[warp] = ended ? 1 : 0;
-                }
+    for (int jr = jtop; jr >= 0; jr -= kSpecRound) {
+        const int nseg = min(kSpecRound, jr + 1);  // segments jr, jr-1, ..., jr-nseg+1
+        for (int i = t; i < nseg * kSpecBands; i += kWideThreads) map[i] = -1;
+        __syncthreads();
+        // ---- speculative walks: thread t takes segment jr - t, its trace bytes from L2
+        if (t < nseg) {
+            const int j = jr - t;
+            const int seg_lo = j * kSpecBands, seg_hi = min(seg_lo + kSpecBands, n_bands);
+            int k = n_kmers - 1, e = best_e;  // the top segment starts at the true start
+            if (j != jtop) {
+                const int sb = min(seg_hi - 1 + kSpecMargin, b0);
+                int kk = bk0[sb] + kBand / 2;  // the middle of band sb, moved inside the read
+                kk = max(kk, max(0, sb - 2 - (n_events - 1)));
+                kk = min(kk, min(n_kmers - 1, sb - 2));
+                k = kk;
+                e = sb - 2 - kk;
             }
-            if (lane == 0) ps.task_idx[warp] = -1;
+            int32_t* row = map + t * kSpecBands;
+            int cnt = 0, ended = 0;
+            while (true) {
+                if ((k | e) < 0) {
+                    ended = 1;
+                    break;
+                }
+                const int band = e + k + 2;
+                if (band < seg_lo) break;
+                const uint32_t f = min((uint32_t)trace[trace_index(band, k & 127)], 2u);
+                if (band < seg_hi) row[band - seg_lo] = k | (cnt++ << 22);
+                k -= (int)((f & 1u) ^ 1u);
+                e -= (int)((f >> 1) ^ 1u);
+            }
+            ps.seg.exit_k[t] = k;
+            ps.seg.exit_e[t] = e;
+            ps.seg.count[t] = cnt;
+            ps.seg.ended[t] = ended;
+            ps.seg.task_idx[t] = -1;
         }
         __syncthreads();
-        // ---- the true path through the window (warp 0, every lane alike)
+        // ---- the true path through the round (warp 0, every lane alike)
         if (warp == 0) {
             int k = ps.k, e = ps.e, n_out = ps.n_out;
             bool done = ps.done != 0;
-            for (int wi = 0; wi < kSpecWarps && !done && jw - wi >= 0; ++wi) {
-                const int seg_lo = (jw - wi) * kSpecBands;
-                const int32_t* spec = spec_mem + wi * kSpecBands;
+            for (int wi = 0; wi < nseg && !done; ++wi) {
+                const int seg_lo = (jr - wi) * kSpecBands;
+                const int32_t* row = map + wi * kSpecBands;
                 while (true) {
                     if ((k | e) < 0) {
                         done = true;
@@ -1669,18 +1677,18 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
                     }
                     const int band = e + k + 2;
                     if (band < seg_lo) break;
-                    const int sp = spec[band - seg_lo];
+                    const int sp = row[band - seg_lo];
                     if (sp >= 0 && (sp & 0x3fffff) == k) {
                         // shared cell: the rest of the segment is the recorded path
                         const int idx = sp >> 22;
                         if (lane == 0) {
-                            ps.task_idx[wi] = idx;
-                            ps.task_off[wi] = n_out;
+                            ps.seg.task_idx[wi] = idx;
+                            ps.seg.task_off[wi] = n_out;
                         }
-                        n_out += ps.count[wi] - idx;
-                        k = ps.exit_k[wi];
-                        e = ps.exit_e[wi];
-                        done = ps.ended[wi] != 0;
+                        n_out += ps.seg.count[wi] - idx;
+                        k = ps.seg.exit_k[wi];
+                        e = ps.seg.exit_e[wi];
+                        done = ps.seg.ended[wi] != 0;
                         break;
                     }
                     const uint32_t f = min((uint32_t)trace[trace_index(band, k & 127)], 2u);
@@ -1698,19 +1706,14 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
             }
         }
         __syncthreads();
-        // ---- the recorded parts, copied by their warps
-        {
-            const int j = jw - warp, idx0 = ps.task_idx[warp];
-            if (j >= 0 && idx0 >= 0) {
-                const int seg_lo = j * kSpecBands, off = ps.task_off[warp];
-                const int32_t* spec = spec_mem + warp * kSpecBands;
-                for (int i = lane; i < kSpecBands; i += 32) {
-                    const int sp = spec[i];
-                    if (sp < 0 || (sp >> 22) < idx0) continue;
-                    const int pos = off + (sp >> 22) - idx0, kk = sp & 0x3fffff;
-                    if (pos < cap) out[pos] = abea_aligned_pair_t{kk, seg_lo + i - 2 - kk};
-                }
-            }
+        // ---- the recorded parts, copied by the block
+        for (int i = t; i < nseg * kSpecBands; i += kWideThreads) {
+            const int wi = i / kSpecBands, idx0 = ps.seg.task_idx[wi];
+            if (idx0 < 0) continue;
+            const int sp = map[i];
+            if (sp < 0 || (sp >> 22) < idx0) continue;
+            const int pos = ps.seg.task_off[wi] + (sp >> 22) - idx0, kk = sp & 0x3fffff;
+            if (pos < cap) out[pos] = abea_aligned_pair_t{kk, (jr - wi) * kSpecBands + (i % kSpecBands) - 2 - kk};
         }
         __syncthreads();
         if (ps.done) break;
@@ -1858,8 +1861,7 @@ static_assert(sizeof(BatchedSmem) <= 227 * 1024, "batched kernel shared memory e
 static_assert(sizeof(WideSmem) >= kPostRingDeep * kPostChunkBands * kSlots && alignof(WideSmem) >= 16,
               "the wide read's traceback ring lives in the wide fill's shared memory");
 static_assert(sizeof(WidePostSmem) <= sizeof(WideSmem), "the wide read's traceback state fits the fill's memory");
-static_assert(sizeof(Rings) * kBatchedWarps >= sizeof(int32_t) * kSpecWarps * kSpecBands,
-              "the speculative segment maps fit the warps' rings");
+
 
 
 template <bool kScores>
@@ -1881,8 +1883,7 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         __syncthreads();
         __threadfence_block();
         // the whole block walks the wide read's traceback (the fill's shared memory is free)
-        post_wide_block<4>(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide),
-                           reinterpret_cast<int32_t*>(sm.warp_rings), sm.post, sm.warp_rings[0], t);
+        post_wide_block(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0], t);
     }
     // phase 2: the first wave is static, the blocks without a wide read taking the
     // longest remaining reads round-robin (warp w of free block f: read f + F*w),
@@ -2169,7 +2170,7 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     noalloc_write_desc<<<1, 1, 0, st>>>(d_desc, desc);
     PreArgs pre{d_desc, 1, g, sequence, events, model, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col};
     CoreArgs core{d_desc, 1, g, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col, trace, nullptr, band_k0,
-                  counters, nullptr, nullptr, 0, nullptr, nullptr, 1ll << 22};
+                  counters, nullptr, nullptr, 0, nullptr, nullptr, nullptr, 0, 1ll << 22};
     PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, km_rsd, last_col, trace, band_k0, pairs, n_pairs, best, status};
     abea_pre_kernel<<<1, 128, 0, st>>>(pre);
     abea_core_warp_kernel<false><<<1, 32, 0, st>>>(core);

@@ -45,6 +45,8 @@ struct CoreArgs {
     int32_t n_wide;                // leading reads of `order` that run on the wide shape
     float* ck;                     // checkpoint records of checkpointed reads
     uint8_t* ck_scratch;           // recompute scratch: kCkBands bands of trace per checkpointed read
+    int32_t* spec;                 // traceback cell maps: kSpecRound * kSpecBands int32 per slot
+    int32_t n_spec;                // slots (queue[2] hands them out)
     long long spin_limit;          // polls before a device-side wait gives up (counters[2] counts those)
 };
 
