@@ -521,10 +521,10 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 struct alignas(16) WideSmem {
     Rings rg;
     float sc[2][kSlots];                       // band scores, buffer b & 1
-    float em[4][kSlots];                       // emission of band b, buffer b & 3
-    float pstep[4][kSlots], wstep[4][kSlots];  // em + step split
-    float pstay[4][kSlots], wstay[4][kSlots];  // em + stay split
-    float magu[4][kSlots];                     // |em| + |stay_h|; NaN when the division is not proven
+    // emission of band b, buffer b & 3: {stay split p, w; |em| + |stay_h| (NaN when the
+    // division is not proven); em} and {step split p, w} (one vector access each)
+    float4 emu[4][kSlots];
+    float2 emd[4][kSlots];
     float dc[2][kSlots];                       // exact diagonal candidate of band b
     int32_t flags[2][kSlots];                  // band b: 1 inside if down, 2 inside if right, 4 d proven
     float trim[2];                             // band b's trim cell value (-inf: outside the read)
@@ -546,12 +546,9 @@ __device__ __forceinline__ void wide_emission(WideSmem& ws, const CellConsts& cc
                                    ws.rg.k1[t], ok);
     const EmSplit s1 = em_split(em, cc.step_h, cc.step_l);
     const EmSplit s2 = em_split(em, cc.stay_h, cc.stay_l);
-    ws.em[buf][t] = em;
-    ws.pstep[buf][t] = s1.p;
-    ws.wstep[buf][t] = s1.w;
-    ws.pstay[buf][t] = s2.p;
-    ws.wstay[buf][t] = s2.w;
-    ws.magu[buf][t] = ok ? __fadd_rn(fabsf(em), fabsf(cc.stay_h)) : __int_as_float(0x7fc00000);
+    ws.emu[buf][t] = make_float4(s2.p, s2.w, ok ? __fadd_rn(fabsf(em), fabsf(cc.stay_h)) : __int_as_float(0x7fc00000),
+                                 em);
+    ws.emd[buf][t] = make_float2(s1.p, s1.w);
 }
 
 // D: band bn's diagonal candidate from `diag`, its inside flags and trim value,
@@ -559,8 +556,9 @@ __device__ __forceinline__ void wide_emission(WideSmem& ws, const CellConsts& cc
 __device__ __forceinline__ void wide_diag(WideSmem& ws, const CellConsts& cc, const GlobalConsts& g, int t, int bn,
                                           float diag, int k0, int n_events, int n_kmers) {
     const int buf = bn & 1, ebuf = bn & 3;
-    const float em = ws.em[ebuf][t];
-    const EmSplit s1{ws.pstep[ebuf][t], ws.wstep[ebuf][t]};
+    const float em = ws.emu[ebuf][t].w;
+    const float2 sd = ws.emd[ebuf][t];
+    const EmSplit s1{sd.x, sd.y};
     bool okd;
     const float d = exact_from_split(diag, s1, __fadd_rn(fabsf(em), fabsf(cc.step_h)), fabsf(em) < INFINITY, okd);
     const int o = (t - k0) & 127;
@@ -654,8 +652,9 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
                 left = ws.sc[pb][(t + 127) & 127];
                 const float d = ws.dc[cb][t];
                 const int f = ws.flags[cb][t];
-                const EmSplit su{ws.pstay[b & 3][t], ws.wstay[b & 3][t]};
-                const float mu = ws.magu[b & 3][t];
+                const float4 eu = ws.emu[b & 3][t];
+                const EmSplit su{eu.x, eu.y};
+                const float mu = eu.z;
                 // up candidate from this slot's own band b-1 score
                 bool oku;
                 const float u = exact_from_split(s_prev, su, mu, mu < INFINITY, oku);
@@ -1858,6 +1857,8 @@ static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSme
                   sizeof(Rings) % 16 == 0 && sizeof(PostSmem) % 16 == 0,
               "cp.async destinations must be 16-byte aligned");
 static_assert(sizeof(BatchedSmem) <= 227 * 1024, "batched kernel shared memory exceeds the per-block limit");
+static_assert(offsetof(WideSmem, emu) % 16 == 0 && offsetof(WideSmem, emd) % 8 == 0,
+              "vector accesses to the emission buffers must be aligned");
 static_assert(sizeof(WideSmem) >= kPostRingDeep * kPostChunkBands * kSlots && alignof(WideSmem) >= 16,
               "the wide read's traceback ring lives in the wide fill's shared memory");
 static_assert(sizeof(WidePostSmem) <= sizeof(WideSmem), "the wide read's traceback state fits the fill's memory");
