@@ -46,7 +46,8 @@ EXPORTS = [
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
     "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
     "abea_batch_backward", "abea_batch_set_scalings", "abea_batch_recalibrate",
-    "abea_align_db", "abea_batch_estimate_scalings", "abea_align_stream",
+    "abea_align_db", "abea_batch_estimate_scalings", "abea_align_stream", "abea_autotune_save",
+    "abea_autotune_load",
 ]
 
 
@@ -144,6 +145,8 @@ def lib():
         L.abea_align_db.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
         L.abea_batch_estimate_scalings.argtypes = [vp, vp, vp, i32]
         L.abea_align_stream.argtypes = [vp, C.POINTER(StreamConfig), i32] + [vp] * 13
+        L.abea_autotune_save.argtypes = [vp, C.c_char_p, C.POINTER(i32)]
+        L.abea_autotune_load.argtypes = [vp, C.c_char_p, C.POINTER(i32)]
         _lib = L
     return _lib
 
@@ -374,6 +377,18 @@ class Context:
                                        _p(sc_out), _p(lat), C.byref(stats)))
         return {"pairs": pairs, "counts": counts[:n], "scalings": sc_out[:n], "latency_ms": lat[:n],
                 "stats": stats.as_dict()}
+
+    def autotune_save(self, path: str) -> int:
+        """Writes the autotuner's results to `path` (abea_autotune_save); returns the entry count."""
+        n = C.c_int32()
+        _check(lib().abea_autotune_save(self.h, os.fsencode(path), C.byref(n)))
+        return n.value
+
+    def autotune_load(self, path: str) -> int:
+        """Merges an autotuner cache file into this context (abea_autotune_load)."""
+        n = C.c_int32()
+        _check(lib().abea_autotune_load(self.h, os.fsencode(path), C.byref(n)))
+        return n.value
 
     def last_timing(self):
         t = Timing()

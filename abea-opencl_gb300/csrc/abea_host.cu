@@ -7,6 +7,7 @@
 // and status codes instead of printing and continuing.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -24,6 +25,14 @@
 #include "abea_launch.h"
 
 using namespace abea;
+
+// NVTX range over a host scope (shown by profilers that record NVTX; a no-op otherwise).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---------------------------------------------------------------- errors
 static thread_local std::string g_last_error;
@@ -620,6 +629,7 @@ static void prepare_order(abea_ctx* c, abea_batch* b) {
 }
 
 static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
+    NvtxRange nv("abea run");
     CUDA_TRY(cudaSetDevice(c->device));
     b->timing = abea_timing_t{};
     if (b->n_reads == 0) {
@@ -688,6 +698,7 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
 // this workload signature (longest read, read count and total bands, log2
 // buckets) and returns it.
 extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* best_threshold, float* best_ms) {
+    NvtxRange nv("abea autotune");
     if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune: null argument");
     if (b->n_reads == 0) return ABEA_OK;
     const abea_mode_t mode0 = c->mode;
@@ -731,6 +742,53 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
     c->tuned[workload_signature(b)] = best;
     if (best_threshold) *best_threshold = best;
     if (best_ms) *best_ms = best_t;
+    return ABEA_OK;
+}
+
+// Autotuner cache: "abea-autotune 1 sm_count <n>" then "<signature> <threshold>" lines.
+extern "C" abea_status_t abea_autotune_save(abea_ctx_t* c, const char* path, int32_t* n_entries) {
+    if (!c || !path) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_save: null argument");
+    FILE* f = fopen(path, "w");
+    if (!f) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_save: cannot open %s", path);
+    fprintf(f, "abea-autotune 1 sm_count %d\n", c->sm_count);
+    for (const auto& kv : c->tuned)
+        fprintf(f, "%llu %lld\n", (unsigned long long)kv.first, (long long)kv.second);
+    const bool ok = fclose(f) == 0;
+    if (!ok) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_save: write to %s failed", path);
+    if (n_entries) *n_entries = (int32_t)c->tuned.size();
+    return ABEA_OK;
+}
+
+extern "C" abea_status_t abea_autotune_load(abea_ctx_t* c, const char* path, int32_t* n_entries) {
+    if (!c || !path) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: null argument");
+    FILE* f = fopen(path, "r");
+    if (!f) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: cannot open %s", path);
+    int version = 0, sm = 0;
+    if (fscanf(f, "abea-autotune %d sm_count %d", &version, &sm) != 2 || version != 1) {
+        fclose(f);
+        return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: %s is not an autotuner cache", path);
+    }
+    if (sm != c->sm_count) {
+        fclose(f);
+        return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: %s was tuned on %d SMs, this device has %d", path,
+                    sm, c->sm_count);
+    }
+    std::map<uint64_t, int64_t> got;
+    unsigned long long sig = 0;
+    long long thr = 0;
+    int r;
+    while ((r = fscanf(f, "%llu %lld", &sig, &thr)) == 2) {
+        if (thr < 1) {
+            fclose(f);
+            return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: bad threshold in %s", path);
+        }
+        got[(uint64_t)sig] = (int64_t)thr;
+    }
+    const bool at_end = r == EOF;
+    fclose(f);
+    if (!at_end) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: malformed line in %s", path);
+    for (const auto& kv : got) c->tuned[kv.first] = kv.second;
+    if (n_entries) *n_entries = (int32_t)got.size();
     return ABEA_OK;
 }
 
@@ -916,6 +974,7 @@ static abea_status_t queue_backward(abea_ctx* c, abea_batch* b, bool model_grad)
 
 extern "C" abea_status_t abea_batch_backward(abea_ctx_t* c, abea_batch_t* b, double* grad_scalings,
                                              double* grad_model, double* path_emission, int32_t* read_status) {
+    NvtxRange nv("abea backward");
     if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_backward: null argument");
     if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
     if (!b->ran) return fail(ABEA_ERR_INVALID_ARG, "batch has not been run");
@@ -999,6 +1058,7 @@ static void gn_step(const abea_batch* b, const double* gn, const int32_t* ast, a
 // equations are taken from the tempered run as they are.
 extern "C" abea_status_t abea_batch_recalibrate(abea_ctx_t* c, abea_batch_t* b, int32_t iterations,
                                                 double first_temperature, abea_scalings_t* out) {
+    NvtxRange nv("abea recalibrate");
     if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_recalibrate: null argument");
     if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
     if (iterations < 0) return fail(ABEA_ERR_INVALID_ARG, "iterations < 0");
@@ -1055,6 +1115,7 @@ extern "C" abea_status_t abea_batch_recalibrate(abea_ctx_t* c, abea_batch_t* b, 
 // ---------------------------------------------------------------- one-call batch
 static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_aligned_pair_t* pairs,
                                       int32_t* n_pairs) {
+    NvtxRange nv("abea align_batch");
     abea_status_t st = validate(in);
     if (st) return st;
     CUDA_TRY(cudaSetDevice(c->device));
@@ -1231,6 +1292,7 @@ extern "C" abea_status_t abea_align_stream(abea_ctx_t* c, const abea_stream_conf
                                            const abea_model_t* model, abea_aligned_pair_t* pairs,
                                            int32_t* n_pairs, abea_scalings_t* scalings_out, double* latency_ms,
                                            abea_stream_stats_t* stats) {
+    NvtxRange nv("abea align_stream");
     using clock = std::chrono::steady_clock;
     const clock::time_point t_call = clock::now();
     if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_align_stream: null context");

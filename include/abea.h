@@ -205,6 +205,14 @@ void abea_batch_destroy(abea_batch_t *batch);
  * Returns the threshold (INT64_MAX = no wide reads) and its time. */
 abea_status_t abea_autotune(abea_ctx_t *ctx, abea_batch_t *batch, int64_t *best_threshold, float *best_ms);
 
+/* The autotuner's results as a text file: a header naming the device's SM count,
+ * then one "signature threshold" line per tuned workload signature.  Loading
+ * merges the file's entries into the context (a file written on a device with
+ * another SM count is refused with ABEA_ERR_INVALID_ARG); *n_entries (may be
+ * NULL) gets the number of entries written or read. */
+abea_status_t abea_autotune_save(abea_ctx_t *ctx, const char *path, int32_t *n_entries);
+abea_status_t abea_autotune_load(abea_ctx_t *ctx, const char *path, int32_t *n_entries);
+
 /* Band matrices of one read after a run, converted to the reference layout
  * (GPU/align_cuda.c:573-583): bands[n_bands*100] scores (needs
  * ABEA_OPT_STORE_SCORES=1, else NULL must be passed), trace[n_bands*100]

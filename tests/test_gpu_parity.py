@@ -268,3 +268,29 @@ def test_wide_shape_block_traceback_on_the_edge_cases(lib, ref_synthetic, thresh
     h = g0.backward()
     assert np.array_equal(g["path_emission"], h["path_emission"])
     assert np.array_equal(g["status"], h["status"])
+
+
+def test_autotuner_cache_round_trip(lib, tmp_path):
+    """abea_autotune_save / abea_autotune_load: the tuned thresholds survive a file;
+    a malformed file or one tuned on another SM count is refused."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("uneven", seed=3)
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    dev = ctx.upload(batch)
+    thr, _ = dev.autotune()
+    path = str(tmp_path / "tuned.txt")
+    assert ctx.autotune_save(path) == 1
+    other = abea.Context(0, abea.MODE_BATCHED)
+    assert other.autotune_load(path) == 1
+    p1, c1 = ctx.align_batch(batch)
+    p2, c2 = other.align_batch(batch)
+    assert_same_alignments(batch, p1, c1, p2, c2)
+    lines = open(path).read().split("\n")
+    assert lines[0].startswith("abea-autotune 1 sm_count ") and lines[1].split()[1] == str(thr)
+    (tmp_path / "bad.txt").write_text("not a cache\n")
+    with pytest.raises(abea.AbeaError):
+        other.autotune_load(str(tmp_path / "bad.txt"))
+    sm = int(lines[0].split()[-1])
+    (tmp_path / "other_gpu.txt").write_text(f"abea-autotune 1 sm_count {sm + 1}\n{lines[1]}\n")
+    with pytest.raises(abea.AbeaError):
+        other.autotune_load(str(tmp_path / "other_gpu.txt"))
