@@ -824,6 +824,7 @@ static abea_status_t check_status(abea_ctx* c, abea_batch* b) {
     CUDA_TRY(cudaMemcpyAsync(cnt, b->d_slow, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     if (cnt[2]) return fail(ABEA_ERR_TIMEOUT, "%llu device-side waits ran out of polls (ABEA_OPT_SPIN_LIMIT)", cnt[2]);
+    if (cnt[3]) return fail(ABEA_ERR_INTERNAL, "%llu device-side stores out of their region (bounds-checked build)", cnt[3]);
     std::vector<int32_t> st((size_t)b->n_reads);
     CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_status, sizeof(int32_t) * st.size(), cudaMemcpyDeviceToHost,
                              c->stream));

@@ -271,8 +271,22 @@ struct FillSpan {
     float* ck_out;
     uint8_t* trace;
     int trace_band0;
+    int trace_tiles;  // 4-band tiles in the trace region (bounds checks)
     bool side;
 };
+
+// Debug builds (ABEA_BOUNDS_CHECK): the global stores of the fill and of the
+// traceback check their index against their region; a store out of it is skipped
+// and counted in counters[3] (the run then reports ABEA_ERR_INTERNAL).
+#ifdef ABEA_BOUNDS_CHECK
+__device__ __forceinline__ bool in_bounds(int64_t i, int64_t n, unsigned long long* counters) {
+    const bool ok = i >= 0 && i < n;
+    if (!ok) atomicAdd(&counters[3], 1ull);
+    return ok;
+}
+#else
+__device__ __forceinline__ bool in_bounds(int64_t, int64_t, unsigned long long*) { return true; }
+#endif
 
 __device__ __forceinline__ FillSpan forward_span(const CoreArgs& a, const ReadDesc& r) {
     FillSpan sp;
@@ -282,6 +296,7 @@ __device__ __forceinline__ FillSpan forward_span(const CoreArgs& a, const ReadDe
     sp.ck_out = r.ck ? a.ck + r.ck_off : nullptr;
     sp.trace = r.ck ? nullptr : a.trace + r.trace_off * kSlots;
     sp.trace_band0 = 0;
+    sp.trace_tiles = r.ck ? 0 : (r.n_bands + 3) / 4;
     sp.side = true;
     return sp;
 }
@@ -298,6 +313,7 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         sp.ck_out = nullptr;
         sp.trace = a.trace + r.trace_off * kSlots;
         sp.trace_band0 = 0;
+        sp.trace_tiles = (r.n_bands + 3) / 4;
         sp.side = true;
     }
     const CellConsts cc = make_consts(r, a.g);
@@ -389,7 +405,8 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
                 best[3] = here ? tv : best[3];
                 word = here ? ((word & 0x00ffffffu) | (in ? (ABEA_FROM_U << 24) : 0u)) : word;
             }
-            if (sp.side && ol >= lo && ol < hi && lane == (sl_last >> 2)) lastc[e0 - ol] = sel4(best, sl_last & 3);
+            if (sp.side && ol >= lo && ol < hi && lane == (sl_last >> 2) && in_bounds(e0 - ol, n_events, a.counters))
+                lastc[e0 - ol] = sel4(best, sl_last & 3);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -403,22 +420,23 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
         tw2 = jb == 2 ? word : tw2;
         tw3 = jb == 3 ? word : tw3;
         if (jb == 3 || b == n_bands - 1) {
-            if (!kSpan || trace)
+            if ((!kSpan || trace) && in_bounds((b - sp.trace_band0) >> 2, sp.trace_tiles, a.counters))
                 reinterpret_cast<uint4*>(trace + (int64_t)((b - sp.trace_band0) >> 2) * 512)[lane] =
                     transpose_bytes(tw0, tw1, tw2, tw3);
             tw0 = tw1 = tw2 = tw3 = 0u;
         }
-        if (kScores && scores)
+        if (kScores && scores && in_bounds(b, r.n_bands, a.counters))
             reinterpret_cast<float4*>(scores + (int64_t)b * kSlots)[lane] = make_float4(best[0], best[1], best[2], best[3]);
         my_k0 = ((b & 31) == lane) ? k0 : my_k0;
         if (sp.side && ((b & 31) == 31 || b == n_bands - 1)) {
-            if (lane <= (b & 31)) bk0[(b & ~31) + lane] = my_k0;
+            if (lane <= (b & 31) && in_bounds((b & ~31) + lane, r.n_bands, a.counters)) bk0[(b & ~31) + lane] = my_k0;
         }
     };
     while (true) {
         bool to_slow = false;
         for (; b < n_bands; ++b) {
-            if (kSpan && sp.ck_out && (b & (kCkBands - 1)) == 0) {
+            if (kSpan && sp.ck_out && (b & (kCkBands - 1)) == 0 &&
+                in_bounds(b / kCkBands, r.n_bands / kCkBands + 1, a.counters)) {
                 // checkpoint s = b / kCkBands: the state this loop resumes from at band b
                 float* rec = sp.ck_out + (int64_t)(b / kCkBands) * kCkStride;
                 reinterpret_cast<float4*>(rec)[lane] = make_float4(S1[0], S1[1], S1[2], S1[3]);
@@ -637,7 +655,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
             from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
             ws.sc[cb][t] = best;
             ws.fr[b & 7][t] = from;
-            if (kScores) scores[(int64_t)b * kSlots + t] = best;
+            if (kScores && in_bounds(b, n_bands, a.counters)) scores[(int64_t)b * kSlots + t] = best;
             lp = left;
             s_prev = best;
         };
@@ -724,9 +742,10 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
                 if (ol < kBand && t == sl_last && bp >= 2) {  // last k-mer column (GPU/align_cuda.cl:722-746)
                     int lo, hi;
                     band_range(kp, ep0, n_events, n_kmers, lo, hi);
-                    if (ol >= lo && ol < hi) lastc[ep0 - ol] = ws.sc[bp & 1][t];
+                    if (ol >= lo && ol < hi && in_bounds(ep0 - ol, n_events, a.counters))
+                        lastc[ep0 - ol] = ws.sc[bp & 1][t];
                 }
-                if (t == 0) bk0[bp] = kp;
+                if (t == 0 && in_bounds(bp, n_bands, a.counters)) bk0[bp] = kp;
                 if ((bp & 3) == 3 || bp == n_bands - 1) {
                     // four bands of backpointers, byte j = band 4q + j (bands past the read: 0)
                     const int q0 = bp & ~3, nj = bp - q0;
@@ -734,7 +753,8 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
                         if (j <= nj) word |= (ws.fr[(q0 + j) & 7][t] & 0xffu) << (8 * j);
-                    reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
+                    if (in_bounds(bp >> 2, (n_bands + 3) / 4, a.counters))
+                        reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
                 }
             }
         }
@@ -974,7 +994,7 @@ __device__ void fill_wide_cl(const CoreArgs& a, const ReadDesc& r, ClSmem& ws, C
                 }
                 ws.sc[cb][t] = best;
                 ws.fr[b & 7][t] = from;
-                if (kScores) scores[(int64_t)b * kSlots + t] = best;
+                if (kScores && in_bounds(b, n_bands, a.counters)) scores[(int64_t)b * kSlots + t] = best;
                 lp = left;
                 s_prev = best;
             };
@@ -1090,16 +1110,18 @@ __device__ void fill_wide_cl(const CoreArgs& a, const ReadDesc& r, ClSmem& ws, C
                 if (ol < kBand && t == sl_last && bp >= 2) {  // last k-mer column (GPU/align_cuda.cl:722-746)
                     int lo, hi;
                     band_range(kp, ep0, n_events, n_kmers, lo, hi);
-                    if (ol >= lo && ol < hi) lastc[ep0 - ol] = ws.sc[bp & 1][t];
+                    if (ol >= lo && ol < hi && in_bounds(ep0 - ol, n_events, a.counters))
+                        lastc[ep0 - ol] = ws.sc[bp & 1][t];
                 }
-                if (t == 0) bk0[bp] = kp;
+                if (t == 0 && in_bounds(bp, n_bands, a.counters)) bk0[bp] = kp;
                 if ((bp & 3) == 3 || bp == n_bands - 1) {
                     const int q0 = bp & ~3, nj = bp - q0;
                     uint32_t word = 0u;
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
                         if (j <= nj) word |= (ws.fr[(q0 + j) & 7][t] & 0xffu) << (8 * j);
-                    reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
+                    if (in_bounds(bp >> 2, (n_bands + 3) / 4, a.counters))
+                        reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
                 }
             }
             cp_async_wait_all();
@@ -1297,6 +1319,7 @@ __device__ __forceinline__ void recompute_segment(const CoreArgs& ca, const Read
     sp.ck_out = nullptr;
     sp.trace = ca.ck_scratch + (int64_t)r.ck_slot * (kCkBands * kSlots);
     sp.trace_band0 = seg * kCkBands;
+    sp.trace_tiles = kCkBands / 4;
     sp.side = false;
     fill_warp<false, true>(ca, r, rg, lane, sp);
     __syncwarp();
@@ -1651,7 +1674,7 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
                 const int band = e + k + 2;
                 if (band < seg_lo) break;
                 const uint32_t f = min((uint32_t)trace[trace_index(band, k & 127)], 2u);
-                if (band < seg_hi) row[band - seg_lo] = k | (cnt++ << 22);
+                if (band < seg_hi && in_bounds(band - seg_lo, kSpecBands, ca.counters)) row[band - seg_lo] = k | (cnt++ << 22);
                 k -= (int)((f & 1u) ^ 1u);
                 e -= (int)((f >> 1) ^ 1u);
             }
