@@ -2195,7 +2195,8 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
     PreArgs pre{d_desc, 1, g, sequence, events, model, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col};
     CoreArgs core{d_desc, 1, g, ev_mean, km_gm, km_sd, km_rsd, km_k1, last_col, trace, nullptr, band_k0,
                   counters, nullptr, nullptr, 0, nullptr, nullptr, nullptr, 0, 1ll << 22};
-    PostArgs post{d_desc, 1, g, ev_mean, km_gm, km_sd, km_k1, km_rsd, last_col, trace, band_k0, pairs, n_pairs, best, status};
+    PostArgs post{d_desc,   1,      g,     ev_mean, km_gm,  km_sd,   km_k1,   km_rsd,  last_col,
+                  trace,    band_k0, pairs, n_pairs, best,   status,  nullptr, nullptr, nullptr};
     abea_pre_kernel<<<1, 128, 0, st>>>(pre);
     abea_core_warp_kernel<false><<<1, 32, 0, st>>>(core);
     abea_post_kernel<<<1, 32, 0, st>>>(core, post);
