@@ -474,6 +474,28 @@ def ours(args, dist):
         un["batched_over_plain"] = un["batched"]["value"] / un["plain"]["value"]
         un["workload"] = WORKLOADS["uneven"]
         out["uneven"] = un
+        # the three batch shapes side by side: batched, plain and the CPU oracle on all host cores
+        per = {}
+        for wl in ("small", "f5c_batch", "uneven"):
+            wb = batch if wl == args.workload else (ub if wl == "uneven" else synth.make_batch(wl, seed=args.seed))
+            wc, wr = wb.band_cells(), wb.n_reads
+            row = {"reads": wr, "band_cells": wc}
+            for name, m in (("batched", pkg.MODE_BATCHED), ("plain", pkg.MODE_PLAIN)):
+                if wl == args.workload and name == args.mode:
+                    ms = ms_per_step
+                elif wl == args.workload:
+                    ms = out[name]["ms_per_step"]
+                elif wl == "uneven":
+                    ms = un[name]["ms_per_step"]
+                else:
+                    ms = statistics.mean(run_mode(pkg, wb, m, device, 3, 1, autotune=args.autotune)["per_step"])
+                row[name] = {"band_cells_per_s": wc / (ms / 1e3), "reads_per_s": wr / (ms / 1e3), "ms": ms}
+            if args.cpu:
+                threads = os.cpu_count() or 1
+                t = cpu_align(wb, threads)
+                row["cpu"] = {"band_cells_per_s": wc / t, "reads_per_s": wr / t, "ms": t * 1e3, "cores": threads}
+            per[wl] = row
+        out["per_config"] = per
     if args.compare and dist.world == 1:
         out["adjoint"] = adjoint_report(pkg, synth, device, args.seed)
     if args.compare and dist.world == 1 and args.serving_mbases > 0:
