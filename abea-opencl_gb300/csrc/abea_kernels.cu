@@ -20,10 +20,15 @@
 // Forms:
 //   plain   — pre, core (warp shape, one block per read), post (one block per
 //             read): the reference's three launches.
-//   batched — pre, then one persistent kernel: each block first takes one of the
-//             longest reads on the wide shape, then its warps pull the remaining
-//             reads longest-first from a device queue; every read's post runs in
-//             the warp that filled it, right after its fill (trace still in L2).
+//   batched — pre, then one persistent kernel of one block per SM: each block
+//             first takes one of the longest reads on the wide shape and walks its
+//             traceback with the whole block (post_wide_block); the blocks without a
+//             wide read take the first wave of the other reads round-robin, one per
+//             warp, and then every warp pulls the rest longest-first from a device
+//             queue; a warp-shape read's post runs in the warp that filled it, right
+//             after its fill (trace still in L2).
+//   The wide shape on a cluster of two blocks (emissions on the second SM) is an
+//   option, measured slower.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
