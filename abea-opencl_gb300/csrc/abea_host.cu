@@ -541,22 +541,70 @@ static int64_t d2h_bytes(const abea_batch* b) {
     return (int64_t)sizeof(abea_aligned_pair_t) * b->pair_cap + (int64_t)sizeof(int32_t) * b->n_reads;
 }
 
+// Heuristic wide-shape threshold: the number n of wide reads (the longest ones
+// whose trace is kept, at most one per block) that minimises an estimate of the
+// batch's makespan, in cycles:
+//   the longest wide read on the wide shape, kWideCyc per band;
+//   the longest warp-shape read: kWarpFloorCyc per band, or kWarpSmCyc per band
+//     times the warps sharing its SM in the first wave (the blocks without a
+//     wide read share the other reads round-robin, at most 16 warps each);
+//   the warp-shape work spread over those blocks, kWarpSmCyc per band per SM.
+// Calibrated on GB300 (the f5c batch, a 1,024-read batch of 1-10 kb reads and the
+// 4,096-read adjoint batch).  Ties go to fewer wide reads; the threshold is the
+// band count of the n-th wide read (none: INT64_MAX).
+static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
+    constexpr double kWideCyc = 510, kWarpFloorCyc = 1440, kWarpSmCyc = 250;
+    const size_t n = b->order.size();
+    std::vector<int64_t> wide_ok;  // band counts of the reads that may be wide, longest first
+    double rest_bands = 0;
+    for (int32_t i : b->order) {
+        const ReadDesc& r = b->reads[(size_t)i];
+        rest_bands += (double)r.n_bands;
+        if (!r.ck) wide_ok.push_back(r.n_bands);
+    }
+    const int max_wide = (int)std::min<size_t>(wide_ok.size(), (size_t)std::max(0, blocks - 1));
+    double best_t = 0;
+    int best_n = 0;
+    int taken = 0;
+    for (int k = 0; k <= max_wide; ++k) {
+        if (k > 0) {  // the k-th wide read leaves the warp-shape set
+            rest_bands -= (double)wide_ok[(size_t)k - 1];
+            ++taken;
+        }
+        // the longest warp-shape read: skip the wide ones (the longest trace-keeping reads)
+        int skip = taken;
+        size_t j = 0;
+        int64_t longest_warp = 0;
+        for (j = 0; j < n; ++j) {
+            const ReadDesc& r = b->reads[(size_t)b->order[j]];
+            if (!r.ck && skip > 0) {
+                --skip;
+                continue;
+            }
+            longest_warp = r.n_bands;
+            break;
+        }
+        const int free_blocks = std::max(1, blocks - k);
+        const double warps = std::min(16.0, std::max(1.0, (double)(n - (size_t)k) / free_blocks));
+        const double t_wide = k > 0 ? (double)wide_ok[0] * kWideCyc : 0.0;
+        const double t_warp = (double)longest_warp * std::max(kWarpFloorCyc, kWarpSmCyc * warps);
+        const double t_work = rest_bands * kWarpSmCyc / free_blocks;
+        const double t = std::max(t_wide, std::max(t_warp, t_work));
+        if (k == 0 || t < best_t * 0.98) {  // a wide read must buy at least 2%
+            best_t = t;
+            best_n = k;
+        }
+    }
+    return best_n > 0 ? wide_ok[(size_t)best_n - 1] : INT64_MAX;
+}
+
 // Reads of the batched form that run on the wide shape: the longest reads over
-// the threshold (the option, the autotuned value, or the heuristic below), at most
+// the threshold (the option, the autotuned value, or the heuristic above), at most
 // one per resident block, never a checkpointed read.  Fills b->dev_order with
 // those reads first, then the rest longest first.
 static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, bool scores, bool cluster) {
     const int blocks = cluster ? sm_count / 2 : batched_blocks_per_sm(scores) * sm_count;
-    int64_t total = 0, longest = 0;
-    for (const ReadDesc& r : b->reads) {
-        total += r.n_bands;
-        longest = std::max<int64_t>(longest, r.n_bands);
-    }
-    // heuristic: a read wider than a warp's even share of the batch, and at least
-    // 30% of the longest read (a warp-shape read shares its SM with 15 others and
-    // runs at ~2,000-3,000 cycles per band, the wide shape at ~510 for one read)
-    if (threshold <= 0)
-        threshold = std::max<int64_t>({1, total / std::max(1, blocks * 8), longest * 3 / 10});
+    if (threshold <= 0) threshold = heuristic_threshold(b, blocks);
     std::vector<int32_t> wide, rest;
     for (int32_t i : b->order) {
         const ReadDesc& r = b->reads[(size_t)i];
@@ -705,11 +753,9 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
     const int64_t thr0 = c->long_read_bands;
     c->mode = ABEA_MODE_BATCHED;
     const int blocks = batched_blocks_per_sm(b->scores_kept) * c->sm_count;
-    int64_t total = 0;
-    for (const ReadDesc& r : b->reads) total += r.n_bands;
     int64_t longest = 0;
     for (const ReadDesc& r : b->reads) longest = std::max<int64_t>(longest, r.n_bands);
-    std::vector<int64_t> cands = {INT64_MAX, std::max<int64_t>({1, total / std::max(1, blocks * 8), longest * 3 / 10})};
+    std::vector<int64_t> cands = {INT64_MAX, heuristic_threshold(b, blocks)};
     for (int num : {1, 2, 3, 4, 6, 8, 12, 16}) {  // the longest num/16 of the resident blocks
         size_t k = std::min<size_t>(b->order.size(), (size_t)std::max(1, blocks * num / 16)) - 1;
         const int64_t c = std::max<int64_t>(1, b->reads[(size_t)b->order[k]].n_bands);
