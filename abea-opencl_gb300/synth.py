@@ -17,6 +17,7 @@ Workloads (reads / length law):
   f5c_batch   1.3 Mbases, lognormal(median 3 kb, sigma 0.6) clipped to [500, 20000]
   uneven      1.3 Mbases, 80% U(200,5000) + 20% U(20000,100000)
   adjoint     4096 reads, U(1000,10000)
+  reads1024   1024 reads, U(1000,10000) (a batch with fewer reads than warps)
   serving     200 Mbases, lognormal(median 8 kb, sigma 0.6) clipped to [500, 200000]
 """
 from __future__ import annotations
@@ -59,6 +60,8 @@ def read_lengths(rng: np.random.Generator, workload: str, target=None) -> np.nda
         return rng.integers(1000, 3001, 64)
     if workload == "adjoint":
         return rng.integers(1000, 10001, 4096)
+    if workload == "reads1024":
+        return rng.integers(1000, 10001, 1024)
     if workload in ("f5c_batch", "uneven", "serving"):
         if target is None:
             target = 200_000_000 if workload == "serving" else 1_300_000

@@ -45,6 +45,7 @@ WORKLOADS = {
     "f5c_batch": "reads totalling 1.3 Mbases, lognormal lengths (median 3 kb, sigma 0.6) clipped to 500 b-20 kb",
     "uneven": "1.3 Mbases: 80% of reads U(200 b, 5 kb), 20% U(20 kb, 100 kb)",
     "small": "64 reads, U(1 kb, 3 kb)",
+    "reads1024": "1,024 reads, U(1 kb, 10 kb) (fewer reads than warps: the throughput regime's latency-bound end)",
 }
 
 
