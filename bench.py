@@ -88,7 +88,8 @@ class Dist:
 
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms; the summary keeps
+    the samples that arrived while the timed region ran (all of them if none did)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -99,11 +100,16 @@ class ClockSampler:
         self.rows = []
         self.proc = None
 
+    def mark(self):
+        """The timed region starts now."""
+        self.t_start = time.perf_counter()
+
     def start(self):
+        self.t_start = time.perf_counter()
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -114,17 +120,21 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
 
     def stop(self) -> dict:
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        time.sleep(0.25)
+        t_end = time.perf_counter()
+        time.sleep(0.1)  # the sample taken as the region ended
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        inside = [r for t, r in self.rows if self.t_start <= t <= t_end + 0.06]
+        rows = inside if inside else [r for _, r in self.rows]
+        self.rows = rows
         sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
@@ -385,6 +395,8 @@ def ours(args, dist):
     cells = batch.band_cells()
     mode = pkg.MODE_BATCHED if args.mode == "batched" else pkg.MODE_PLAIN
 
+    clocks = ClockSampler(device)
+    clocks.start()  # nvidia-smi starts sampling during the setup; the summary keeps the timed region
     ctx = pkg.Context(device, mode)
     dev = ctx.upload(batch)
     tuned = None
@@ -395,8 +407,7 @@ def ours(args, dist):
         dev.run()
         dev.sync()
     dist.barrier()
-    clocks = ClockSampler(device)
-    clocks.start()
+    clocks.mark()
     t_wall0 = time.perf_counter()
     per_step, core = [], []
     for _ in range(args.steps):
