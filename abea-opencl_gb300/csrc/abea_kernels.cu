@@ -1202,20 +1202,20 @@ struct Walk {
     double sum;  // emissions of the walked cells in walk order (kSum)
 };
 
-// Walks the path from (w.k, w.e) while its band is >= band_lo.  The trace tiles
-// come from `trace` (band trace_band0 at its start; bands below bands_end exist)
-// through a shared-memory ring of four 16-band chunks (band B at ring band
-// B & 63): the chunk being walked and the one below it resident, the two below
-// those in flight.  Each walk iteration loads the bytes of the current cell and
-// of its three possible predecessors at once and takes two steps; the moves are
-// decoded arithmetically (D = 0, U = 1, L = 2: the k-mer steps back unless U,
-// the event unless L).  Cells go to out (capacity cap) or, with kSum, their
-// emissions into w.sum.  Every lane calls it; lane 0 walks.  Returns true once
-// the path has ended (k or e below 0); false when it left the segment.
 // What a walk does with each cell: store the pair, sum its emission (walk
 // order), or record it in a speculative segment map (spec[band - band_lo] =
 // k | index << 22 for the cells below band spec_hi).
 enum WalkMode { kWalkPairs = 0, kWalkSum = 1, kWalkSpec = 2 };
+
+// Walks the path from (w.k, w.e) while its band is >= band_lo.  The trace tiles
+// come from `trace` (band trace_band0 at its start; bands below bands_end exist)
+// through a shared-memory ring of kRing 16-band chunks: the chunk being walked
+// and the one below it resident, the others in flight.  Each round of loads
+// takes the backpointers of the nine cells two moves can reach and takes up to
+// three steps from them; the moves are decoded arithmetically (D = 0, U = 1,
+// L = 2: the k-mer steps back unless U, the event unless L).  Every lane walks
+// the same path; lane 0 stores.  Returns true once the path has ended (k or e
+// below 0); false when it left the segment.
 
 template <int kMode, int kRing>
 __device__ bool walk_segment(const uint8_t* trace, int trace_band0, int bands_end, int band_lo, uint8_t* ring,

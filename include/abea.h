@@ -90,9 +90,11 @@ typedef enum {
  *  PLAIN   — the reference's structure: three kernels (pre, core, post) launched
  *            one after the other, one thread block per read, full score and
  *            trace matrices in HBM (GPU/align_cuda.c:680-850).
- *  BATCHED — one persistent kernel per stage pulling reads longest-first from a
- *            device work queue, several threads-per-band shapes chosen per
- *            length bucket, all three stages replayed as one CUDA graph. */
+ *  BATCHED — pre, then one persistent kernel (fill and traceback fused) of one
+ *            block per SM: the longest reads on a 512-thread shape (their
+ *            traceback walked by the whole block), the rest one warp each, first
+ *            spread round-robin over the blocks, then pulled longest-first from a
+ *            device queue; replayed as one CUDA graph. */
 typedef enum { ABEA_MODE_PLAIN = 0, ABEA_MODE_BATCHED = 1 } abea_mode_t;
 
 /* Context options (abea_ctx_set_option). */
