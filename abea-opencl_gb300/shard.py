@@ -32,3 +32,17 @@ def load_per_rank(n_bands, world: int) -> np.ndarray:
     n_bands = np.asarray(n_bands, dtype=np.int64)
     own = owners(n_bands, world)
     return np.array([int(n_bands[own == r].sum()) for r in range(world)], dtype=np.int64)
+
+
+def reduce_model_gradient(grad_model):
+    """Sums the adjoint's pore-model gradient (4096 x 2 FP64, one per rank's shard)
+    over the ranks of the default torch.distributed process group: the one
+    collective of a sharded run, 64 KB per batch.  The per-read gradients stay
+    with their shard."""
+    import torch
+    import torch.distributed as dist
+    t = torch.from_numpy(np.ascontiguousarray(grad_model, dtype=np.float64).copy())
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return t.cpu().numpy()

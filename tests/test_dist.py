@@ -86,3 +86,50 @@ def test_shards_balance_band_cells():
         load = load_per_rank(nb, world)
         # LPT: no rank exceeds the mean by more than the longest read
         assert load.max() <= load.mean() + nb.max()
+
+
+def _adjoint_worker(rank, world, port, out_dir):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import sys
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import load_package
+    load_package()
+    from abea_gb300 import synth
+    from abea_gb300.shard import reduce_model_gradient, shard_reads
+    from oracle import oracle
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    batch = synth.make_batch("small", seed=9, lengths=np.random.default_rng(6).integers(300, 1200, 8))
+    gm = np.zeros((4096, 2))
+    for i in shard_reads(batch.n_bands(), world, rank):
+        seq = bytes(batch.read[batch.read_ptr[i]:batch.read_ptr[i] + batch.read_len[i]])
+        ev = batch.events[batch.event_ptr[i]:batch.event_ptr[i] + batch.n_events[i]]
+        _, _, info = oracle.align(seq, ev, batch.model, batch.scalings[i], 0)
+        gm += oracle.path_adjoint(info["walk"], info["last_from"], seq, ev, batch.model, batch.scalings[i], 0,
+                                  want_model=True)[3]
+    total = reduce_model_gradient(gm)
+    if rank == 0:
+        np.save(os.path.join(out_dir, "gm.npy"), total)
+    dist.destroy_process_group()
+
+
+def test_two_rank_model_gradient_reduction(tmp_path, oracle_mod):
+    """A sharded adjoint: each rank sums the FP64 model gradient of its reads, one
+    all-reduce gives the whole batch's (equal to one process's up to the order of
+    the FP64 sums)."""
+    world = 2
+    mp.start_processes(_adjoint_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True,
+                       start_method="spawn")
+    total = np.load(os.path.join(tmp_path, "gm.npy"))
+    from abea_gb300 import synth
+    batch = synth.make_batch("small", seed=9, lengths=np.random.default_rng(6).integers(300, 1200, 8))
+    ref = np.zeros((4096, 2))
+    for i in range(batch.n_reads):
+        seq = bytes(batch.read[batch.read_ptr[i]:batch.read_ptr[i] + batch.read_len[i]])
+        ev = batch.events[batch.event_ptr[i]:batch.event_ptr[i] + batch.n_events[i]]
+        _, _, info = oracle_mod.align(seq, ev, batch.model, batch.scalings[i], 0)
+        ref += oracle_mod.path_adjoint(info["walk"], info["last_from"], seq, ev, batch.model, batch.scalings[i], 0,
+                                       want_model=True)[3]
+    assert np.count_nonzero(ref) > 0
+    assert np.allclose(total, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
