@@ -47,7 +47,7 @@ EXPORTS = [
     "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
     "abea_batch_backward", "abea_batch_set_scalings", "abea_batch_recalibrate",
     "abea_align_db", "abea_batch_estimate_scalings", "abea_align_stream", "abea_autotune_save",
-    "abea_autotune_load",
+    "abea_autotune_load", "abea_align_batch_persistent", "abea_backward_batch",
 ]
 
 
@@ -118,6 +118,8 @@ def lib():
         L.abea_align_cap.argtypes = [vp, i32, C.c_char_p, i32, vp, i32, vp, _Scalings]
         L.abea_align_cap.restype = i32
         L.abea_align_batch.argtypes = [vp, i32] + [vp] * 10
+        L.abea_align_batch_persistent.argtypes = [vp, i32] + [vp] * 10
+        L.abea_backward_batch.argtypes = [vp, vp, vp, vp, vp, vp]
         L.abea_batch_create.argtypes = [vp, i32] + [vp] * 8 + [C.POINTER(vp)]
         L.abea_batch_run.argtypes = [vp, vp]
         L.abea_batch_sync.argtypes = [vp]

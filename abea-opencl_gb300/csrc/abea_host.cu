@@ -1049,6 +1049,11 @@ extern "C" abea_status_t abea_batch_backward(abea_ctx_t* c, abea_batch_t* b, dou
     return ABEA_OK;
 }
 
+extern "C" abea_status_t abea_backward_batch(abea_ctx_t* c, abea_batch_t* b, double* grad_scalings,
+                                             double* grad_model, double* path_emission, int32_t* read_status) {
+    return abea_batch_backward(c, b, grad_scalings, grad_model, path_emission, read_status);
+}
+
 // Host copy of the per-read scalings -> descriptors (and their shortcut flag).
 static void apply_scalings(abea_batch* b, const abea_scalings_t* sc) {
     for (int32_t i = 0; i < b->n_reads; ++i) {
@@ -1201,6 +1206,22 @@ extern "C" abea_status_t abea_align_batch(abea_ctx_t* c, int32_t n_reads, const 
         return fail(ABEA_ERR_INVALID_ARG, "abea_align_batch: null output");
     HostInputs in = inputs(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model);
     return align_batch_impl(c, in, event_align_pairs, n_event_align_pairs);
+}
+
+extern "C" abea_status_t abea_align_batch_persistent(abea_ctx_t* c, int32_t n_reads, const char* read,
+                                                     const int64_t* read_ptr, const int32_t* read_len,
+                                                     const abea_event_t* event_table, const int64_t* event_ptr,
+                                                     const int32_t* n_events, const abea_scalings_t* scalings,
+                                                     const abea_model_t* model,
+                                                     abea_aligned_pair_t* event_align_pairs,
+                                                     int32_t* n_event_align_pairs) {
+    if (!c) return fail(ABEA_ERR_INVALID_ARG, "abea_align_batch_persistent: null context");
+    const abea_mode_t mode0 = c->mode;
+    c->mode = ABEA_MODE_BATCHED;
+    const abea_status_t st = abea_align_batch(c, n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events,
+                                              scalings, model, event_align_pairs, n_event_align_pairs);
+    c->mode = mode0;
+    return st;
 }
 
 // f5c's db_t arrays: flatten into pinned staging (GPU/align_cuda.c:432-497's layout),

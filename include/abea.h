@@ -174,6 +174,15 @@ abea_status_t abea_align_batch(abea_ctx_t *ctx, int32_t n_reads, const char *rea
                                const abea_model_t *model, abea_aligned_pair_t *event_align_pairs,
                                int32_t *n_event_align_pairs);
 
+/* abea_align_batch in the batched form whatever the context's ABEA_OPT_MODE: the
+ * persistent kernel over the device work queue, replayed as one CUDA graph. */
+abea_status_t abea_align_batch_persistent(abea_ctx_t *ctx, int32_t n_reads, const char *read,
+                                          const int64_t *read_ptr, const int32_t *read_len,
+                                          const abea_event_t *event_table, const int64_t *event_ptr,
+                                          const int32_t *n_events, const abea_scalings_t *scalings,
+                                          const abea_model_t *model, abea_aligned_pair_t *event_align_pairs,
+                                          int32_t *n_event_align_pairs);
+
 /* f5c's per-read arrays (db_t's read[i], read_len[i], et[i], scalings[i],
  * event_align_pairs[i], n_event_align_pairs[i]; GPU/f5c.h) aligned as one batch:
  * the flattening of GPU/align_cuda.c:432-497 done inside the library, through
@@ -278,6 +287,9 @@ abea_status_t abea_selftest_arith(int64_t cases, uint64_t seed, int64_t *out);
  * Reads whose alignment failed the quality checks still have a path and a
  * gradient. */
 abea_status_t abea_batch_backward(abea_ctx_t *ctx, abea_batch_t *batch, double *grad_scalings,
+                                  double *grad_model, double *path_emission, int32_t *read_status);
+/* The same entry under the name of the batch-form plan (abea_backward_batch). */
+abea_status_t abea_backward_batch(abea_ctx_t *ctx, abea_batch_t *batch, double *grad_scalings,
                                   double *grad_model, double *path_emission, int32_t *read_status);
 
 /* Replaces the per-read scalings of a device-resident batch (host array

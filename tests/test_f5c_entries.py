@@ -77,3 +77,29 @@ def test_gpu_mom_matches_the_oracle_and_seeds_recalibration(oracle_mod):
     fit = dev.recalibrate(3, first_temperature=5.0)
     ok = (np.abs(fit["shift"] - true["shift"]) < 1.0) & (np.abs(fit["scale"] / true["scale"] - 1) < 0.01)
     assert ok.mean() >= 0.9, ok.mean()
+
+
+@pytest.mark.gpu
+def test_persistent_and_backward_entries(oracle_mod):
+    """abea_align_batch_persistent runs the batched form from a plain context;
+    abea_backward_batch is abea_batch_backward."""
+    import ctypes as C
+    from abea_gb300 import synth
+    batch = synth.make_batch("small", seed=12)
+    ctx = abea.Context(0, abea.MODE_PLAIN)
+    arrs = abea._batch_arrays(batch)
+    pairs = np.zeros(max(batch.pair_capacity(), 1), dtype=abea.types.PAIR_DTYPE)
+    counts = np.zeros(batch.n_reads, dtype=np.int32)
+    abea._check(abea.lib().abea_align_batch_persistent(ctx.h, batch.n_reads, *[abea._p(a) for a in arrs],
+                                                       abea._p(pairs), abea._p(counts)))
+    assert ctx.get_option(abea.OPT_MODE) == abea.MODE_PLAIN
+    op, oc, _ = oracle_mod.align_batch(batch, threads=os.cpu_count())
+    assert np.array_equal(counts, oc)
+    for x, y in zip(abea.split_pairs(batch, pairs, counts), abea.split_pairs(batch, op, oc)):
+        assert np.array_equal(x, y)
+    dev = abea.Context(0, abea.MODE_BATCHED).upload(batch)
+    dev.run()
+    g = dev.backward(model_grad=False)
+    g2 = np.zeros((batch.n_reads, 3))
+    abea._check(abea.lib().abea_backward_batch(dev.ctx.h, dev.h, abea._p(g2), None, None, None))
+    assert np.array_equal(g["grad_scalings"], g2)
