@@ -72,3 +72,21 @@ def test_serving_stream_full_size_forms_agree():
     # the step moved the scalings towards the generating ones
     true = batch.meta["true_scalings"]
     assert np.median(np.abs(s1["shift"] - true["shift"])) < 0.5
+
+
+def test_exact_against_the_oracle_over_a_billion_band_cells(oracle_mod):
+    """The exact FP32 evaluation of the reference's double arithmetic, checked on
+    more than 10^9 band cells: the reads1024 workload (1,024 reads of 1-10 kb,
+    1.5x10^9 band cells) in the batched form against the CPU oracle on all host
+    cores: AlignedPairs and best-end scores bit-exact."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("reads1024", seed=2)
+    assert batch.band_cells() > 10**9
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    best = dev.best_scores()
+    op, oc, obest = oracle_mod.align_batch(batch, threads=os.cpu_count())
+    same_pairs(batch, gp, gc, op, oc)
+    assert np.array_equal(best.view(np.uint32), np.asarray(obest, dtype=np.float32).view(np.uint32))
