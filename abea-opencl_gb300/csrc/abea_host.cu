@@ -129,6 +129,7 @@ struct abea_batch {
     cudaGraphExec_t graph = nullptr;  // batched form: memsets + pre + fused core/post
     std::vector<uint64_t> carve;      // slab base and region sizes: every device pointer follows from them
     std::vector<uint64_t> graph_key;  // what the captured graph's launch arguments were built from
+    int graph_launches = 0;           // kernels in the captured graph
 };
 
 struct abea_ctx {
@@ -723,8 +724,9 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
                 return fail(ABEA_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
             }
             b->graph_key = key;
+            b->graph_launches = launches;
         }
-        launches = 2;
+        launches = b->graph_launches;
         CUDA_TRY(cudaEventRecord(c->ev[0], c->stream));
         CUDA_TRY(cudaGraphLaunch(b->graph, c->stream));
         CUDA_TRY(cudaEventRecord(c->ev[3], c->stream));

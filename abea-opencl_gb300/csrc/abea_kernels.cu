@@ -20,7 +20,8 @@
 // Forms:
 //   plain   — pre, core (warp shape, one block per read), post (one block per
 //             read): the reference's three launches.
-//   batched — pre, then one persistent kernel of one block per SM: each block
+//   batched — one persistent kernel of one block per SM (each read's pre runs
+//             in the block or warp that fills it): each block
 //             first takes one of the longest reads on the wide shape and walks its
 //             traceback with the whole block (post_wide_block); the blocks without a
 //             wide read take the first wave of the other reads round-robin, one per
@@ -88,14 +89,15 @@ __device__ __forceinline__ CellConsts make_consts(const ReadDesc& r, const Globa
 
 // ---------------------------------------------------------------- pre
 // One block per read; thread t handles k-mer positions t, t+blockDim, ...
-__global__ void __launch_bounds__(128) abea_pre_kernel(PreArgs a) {
-    int i = blockIdx.x;
-    if (i >= a.n_reads) return;
+// Pre of read i by nt cooperating threads (thread index t): the read's k-mer
+// parameters, event means and last-column initialisation.  The batched form runs
+// it in the block or warp that fills the read, just before the fill.
+__device__ __forceinline__ void pre_read(const PreArgs& a, int i, int t, int nt) {
     const ReadDesc r = a.reads[i];
     if (r.skip) return;
     const char* s = a.seq + r.seq_off;
     const int nk = r.n_kmers, nk_pad = round_up_dev(nk);
-    for (int k = threadIdx.x; k < nk_pad; k += blockDim.x) {
+    for (int k = t; k < nk_pad; k += nt) {
         float gm = 0.f, sd = 1.f, rsd = 1.f, k1 = 0.f;
         if (k < nk) {
             uint32_t rank = 0;
@@ -120,10 +122,16 @@ __global__ void __launch_bounds__(128) abea_pre_kernel(PreArgs a) {
         a.km_k1[r.km_off + k] = k1;
     }
     const int ne = r.n_events, ne_pad = round_up_dev(ne);
-    for (int e = threadIdx.x; e < ne_pad; e += blockDim.x) {
+    for (int e = t; e < ne_pad; e += nt) {
         a.ev_mean[r.ev_off + e] = e < ne ? a.ev_in[r.ev_src + e].mean : 0.f;
         a.last_col[r.ev_off + e] = -INFINITY;
     }
+}
+
+__global__ void __launch_bounds__(128) abea_pre_kernel(PreArgs a) {
+    const int i = blockIdx.x;
+    if (i >= a.n_reads) return;
+    pre_read(a, i, threadIdx.x, blockDim.x);
 }
 
 // ---------------------------------------------------------------- prefetch rings
@@ -1894,7 +1902,7 @@ static_assert(sizeof(WidePostSmem) <= sizeof(WideSmem), "the wide read's traceba
 
 
 template <bool kScores>
-__global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs a, PostArgs p) {
+__global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs a, PostArgs p, PreArgs pa) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchedSmem& sm = *reinterpret_cast<BatchedSmem*>(smem_raw);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -1908,6 +1916,8 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
     const int wide_read = sm.pick, free_rank = sm.free_rank;
     if (wide_read >= 0) {
         const ReadDesc& r = a.reads[wide_read];
+        pre_read(pa, wide_read, t, kWideThreads);
+        __syncthreads();  // the read's parameters are in memory for the whole block
         if (!r.skip) fill_wide<kScores>(a, r, sm.wide, t);
         __syncthreads();
         __threadfence_block();
@@ -1935,6 +1945,8 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         }
         const int ri = a.order[a.n_wide + q];
         const ReadDesc& r = a.reads[ri];
+        pre_read(pa, ri, lane, 32);
+        __syncwarp();  // the read's parameters are in memory for the warp
         if (!r.skip) {
             if (r.ck)
                 fill_warp<kScores, true>(a, r, sm.warp_rings[warp], lane, forward_span(a, r));
@@ -2056,7 +2068,7 @@ static int cl_max_dyn_smem_set() {
 
 cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
     const int n = la.core.n_reads;
-    abea_pre_kernel<<<n, 128, 0, la.stream>>>(la.pre);
+    if (la.cluster) abea_pre_kernel<<<n, 128, 0, la.stream>>>(la.pre);  // otherwise pre runs inside the kernel
     cudaEventRecordWithFlags(la.ev_pre, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     const bool scores = la.core.scores != nullptr;
     if (la.cluster) {
@@ -2079,11 +2091,11 @@ cudaError_t launch_batched(const LaunchArgs& la, int* launches) {
     const int grid = std::max(1, std::min(max_blocks, n));
     const size_t smem = sizeof(BatchedSmem);
     if (scores)
-        abea_batched_kernel<true><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
+        abea_batched_kernel<true><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post, la.pre);
     else
-        abea_batched_kernel<false><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post);
+        abea_batched_kernel<false><<<grid, kWideThreads, smem, la.stream>>>(la.core, la.post, la.pre);
     cudaEventRecordWithFlags(la.ev_core, la.stream, la.capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
-    *launches = 2;
+    *launches = 1;
     return cudaGetLastError();
 }
 

@@ -90,7 +90,7 @@ typedef enum {
  *  PLAIN   — the reference's structure: three kernels (pre, core, post) launched
  *            one after the other, one thread block per read, full score and
  *            trace matrices in HBM (GPU/align_cuda.c:680-850).
- *  BATCHED — pre, then one persistent kernel (fill and traceback fused) of one
+ *  BATCHED — one persistent kernel (pre, fill and traceback fused) of one
  *            block per SM: the longest reads on a 512-thread shape (their
  *            traceback walked by the whole block), the rest one warp each, first
  *            spread round-robin over the blocks, then pulled longest-first from a

@@ -206,7 +206,7 @@ def test_autotuned_batched_stays_exact(lib, oracle_mod):
     assert thr > 0 and ms > 0
     dev.run()
     gp, gc = dev.results()
-    assert dev.timing()["kernel_launches"] == 2  # pre + fused core/post, one graph
+    assert dev.timing()["kernel_launches"] == 1  # pre, fill and traceback fused, one graph
     op, oc, _ = oracle_batch(oracle_mod, batch)
     assert_same_alignments(batch, gp, gc, op, oc)
 
