@@ -22,8 +22,8 @@ import weakref
 import numpy as np
 
 from . import types
-from .types import (BANDWIDTH, EKPAIR_DTYPE, EVENT_DTYPE, MODEL_DTYPE, PAIR_DTYPE, SCALINGS_DTYPE,
-                    Batch, from_reads, split_pairs)
+from .types import (BANDWIDTH, EKPAIR_DTYPE, EVENT_ALIGNMENT_DTYPE, EVENT_DTYPE, INDEX_PAIR_DTYPE, MODEL_DTYPE,
+                    PAIR_DTYPE, SCALINGS_DTYPE, Batch, from_reads, split_pairs, split_postalign)
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libabea.so")
@@ -46,7 +46,7 @@ EXPORTS = [
     "abea_ctx_last_timing", "abea_batch_io_bytes", "abea_ctx_mark", "abea_ctx_elapsed",
     "abea_ctx_flush_l2", "abea_selftest_arith", "abea_align_noalloc", "abea_autotune",
     "abea_batch_backward", "abea_batch_set_scalings", "abea_batch_recalibrate",
-    "abea_align_db", "abea_batch_estimate_scalings", "abea_align_stream", "abea_autotune_save",
+    "abea_align_db", "abea_batch_estimate_scalings", "abea_batch_postalign", "abea_align_stream", "abea_autotune_save",
     "abea_autotune_load", "abea_align_batch_persistent", "abea_backward_batch",
 ]
 
@@ -146,6 +146,7 @@ def lib():
         L.abea_batch_recalibrate.argtypes = [vp, vp, i32, C.c_double, vp]
         L.abea_align_db.argtypes = [vp, i32, vp, vp, vp, vp, vp, vp, vp]
         L.abea_batch_estimate_scalings.argtypes = [vp, vp, vp, i32]
+        L.abea_batch_postalign.argtypes = [vp, vp, vp, vp, vp, vp]
         L.abea_align_stream.argtypes = [vp, C.POINTER(StreamConfig), i32] + [vp] * 13
         L.abea_autotune_save.argtypes = [vp, C.c_char_p, C.POINTER(i32)]
         L.abea_autotune_load.argtypes = [vp, C.c_char_p, C.POINTER(i32)]
@@ -261,6 +262,24 @@ class DeviceBatch:
         out = np.zeros(max(self.batch.n_reads, 1), dtype=SCALINGS_DTYPE)
         _check(lib().abea_batch_estimate_scalings(self.ctx.h, self.h, _p(out), 1 if apply else 0))
         return out[: self.batch.n_reads]
+
+    def postalign(self):
+        """f5c's postalign for every read of the last run (abea_batch_postalign):
+        dict with alignment [events] (EVENT_ALIGNMENT_DTYPE, read i's records from
+        event_ptr[i]), base_to_event_map [read buffer] (INDEX_PAIR_DTYPE, read i's
+        n_kmers entries from read_ptr[i]), events_per_base [n] and n_alignment [n];
+        `split_postalign` cuts them per read."""
+        b = self.batch
+        n = b.n_reads
+        n_rec = int((b.event_ptr + b.n_events).max()) if n else 0
+        n_map = int((b.read_ptr + b.read_len + 1).max()) if n else 0
+        rec = np.zeros(max(n_rec, 1), dtype=EVENT_ALIGNMENT_DTYPE)
+        bmap = np.zeros(max(n_map, 1), dtype=INDEX_PAIR_DTYPE)
+        epb = np.zeros(max(n, 1))
+        cnt = np.zeros(max(n, 1), dtype=np.int32)
+        _check(lib().abea_batch_postalign(self.ctx.h, self.h, _p(rec), _p(bmap), _p(epb), _p(cnt)))
+        return dict(alignment=rec[:n_rec], base_to_event_map=bmap[:n_map], events_per_base=epb[:n],
+                    n_alignment=cnt[:n])
 
     def set_scalings(self, scalings):
         sc = np.ascontiguousarray(scalings, dtype=SCALINGS_DTYPE)
@@ -445,6 +464,6 @@ def version() -> str:
     return lib().abea_version().decode()
 
 
-__all__ = ["align", "Context", "DeviceBatch", "Batch", "from_reads", "split_pairs", "build", "lib",
+__all__ = ["align", "Context", "DeviceBatch", "Batch", "from_reads", "split_pairs", "split_postalign", "build", "lib",
            "AbeaError", "MODE_PLAIN", "MODE_BATCHED", "types", "EXPORTS", "version",
            "selftest_arith", "pinned_empty", "pin_batch", "StreamConfig", "StreamStats"]

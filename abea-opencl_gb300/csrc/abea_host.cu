@@ -130,6 +130,8 @@ struct abea_batch {
     std::vector<uint64_t> carve;      // slab base and region sizes: every device pointer follows from them
     std::vector<uint64_t> graph_key;  // what the captured graph's launch arguments were built from
     int graph_launches = 0;           // kernels in the captured graph
+    void* d_post = nullptr;           // abea_batch_postalign's outputs (allocated on first use)
+    size_t post_bytes = 0;
 };
 
 struct abea_ctx {
@@ -195,6 +197,9 @@ static void free_batch_device(abea_batch* b) {
     b->graph = nullptr;
     if (b->slab.base) cudaFree(b->slab.base);
     b->slab = DevSlab{};
+    if (b->d_post) cudaFree(b->d_post);
+    b->d_post = nullptr;
+    b->post_bytes = 0;
 }
 
 extern "C" void abea_batch_destroy(abea_batch_t* b) {
@@ -1304,6 +1309,66 @@ extern "C" abea_status_t abea_batch_estimate_scalings(abea_ctx_t* c, abea_batch_
         apply_scalings(b, sc.data());
         return upload_reads(c, b);
     }
+    return ABEA_OK;
+}
+
+// f5c's postalign for every read of a run batch, on the AlignedPairs in HBM.
+extern "C" abea_status_t abea_batch_postalign(abea_ctx_t* c, abea_batch_t* b, abea_event_alignment_t* alignment,
+                                              abea_index_pair_t* base_to_event_map, double* events_per_base,
+                                              int32_t* n_alignment) {
+    if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_batch_postalign: null argument");
+    if (b->ctx != c) return fail(ABEA_ERR_INVALID_ARG, "batch belongs to another context");
+    if (!b->ran) return fail(ABEA_ERR_INVALID_ARG, "batch has not been run");
+    if (b->n_reads == 0) return ABEA_OK;
+    NvtxRange nv("abea postalign");
+    CUDA_TRY(cudaSetDevice(c->device));
+    const size_t n = (size_t)b->n_reads;
+    const size_t n_rec = (size_t)std::max<int64_t>(b->n_events_total, 1);
+    const size_t n_map = (size_t)std::max<int64_t>(b->seq_bytes, 1);
+    const size_t rec_bytes = sizeof(abea_event_alignment_t) * n_rec, map_bytes = sizeof(abea_index_pair_t) * n_map;
+    const size_t off_map = (size_t)round_up((int64_t)rec_bytes, 256);
+    const size_t off_epb = off_map + (size_t)round_up((int64_t)map_bytes, 256);
+    const size_t off_cnt = off_epb + (size_t)round_up((int64_t)(sizeof(double) * n), 256);
+    const size_t need = off_cnt + sizeof(int32_t) * n;
+    if (b->post_bytes < need) {
+        if (b->d_post) cudaFree(b->d_post);
+        b->d_post = nullptr;
+        b->post_bytes = 0;
+        if (cudaMalloc(&b->d_post, need) != cudaSuccess) {
+            cudaGetLastError();
+            b->d_post = nullptr;
+            return fail(ABEA_ERR_OUT_OF_MEMORY, "postalign outputs: cannot allocate %zu bytes", need);
+        }
+        b->post_bytes = need;
+    }
+    char* base = (char*)b->d_post;
+    PostalignArgs pa{b->d_reads,
+                     b->n_reads,
+                     b->d_seq,
+                     b->d_pairs,
+                     b->d_n_pairs,
+                     (abea_index_pair_t*)(base + off_map),
+                     (abea_event_alignment_t*)base,
+                     (double*)(base + off_epb),
+                     (int32_t*)(base + off_cnt)};
+    CUDA_TRY(cudaMemsetAsync(pa.rec, 0, rec_bytes, c->stream));
+    CUDA_TRY(cudaMemsetAsync(pa.map, 0xff, map_bytes, c->stream));  // {-1, -1}
+    cudaError_t e = launch_postalign(pa, c->stream);
+    if (e != cudaSuccess) return fail(ABEA_ERR_CUDA, "postalign kernel launch failed: %s", cudaGetErrorString(e));
+    std::vector<int32_t> cnt(n);
+    if (alignment)
+        CUDA_TRY(cudaMemcpyAsync(alignment, pa.rec, sizeof(abea_event_alignment_t) * (size_t)b->n_events_total,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    if (base_to_event_map)
+        CUDA_TRY(cudaMemcpyAsync(base_to_event_map, pa.map, sizeof(abea_index_pair_t) * (size_t)b->seq_bytes,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    if (events_per_base)
+        CUDA_TRY(cudaMemcpyAsync(events_per_base, pa.epb, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(cnt.data(), pa.count, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (n_alignment) memcpy(n_alignment, cnt.data(), sizeof(int32_t) * n);
+    for (size_t i = 0; i < n; ++i)
+        if (cnt[i] < 0) return fail(ABEA_ERR_INTERNAL, "read %zu: its AlignedPairs are not a path of unit steps", i);
     return ABEA_OK;
 }
 

@@ -2365,3 +2365,116 @@ cudaError_t launch_mom(const MomArgs& a, cudaStream_t stream) {
 }
 
 }  // namespace abea
+
+// ---------------------------------------------------------------- postalign
+// f5c's postalign (GPU/f5cmisc.h:51-52, prototype only; the output types are
+// GPU/f5c.h:184-207): the AlignedPairs of a read turned into its base-to-event
+// map and its event alignment records.  One warp per read over the pairs in
+// order, 32 at a time.
+//
+// A pair counts for its k-mer when its event differs from the previous pair's;
+// such a pair is the first one of its event on the path.  The traceback's path
+// moves by one k-mer, one event or both at every step, so the counting pairs
+// are exactly one per event from the first event on the path to the last, in
+// order: the record of event e sits at e - first event, and a k-mer's map
+// entry runs from its first counting pair's event to its last one's.  The first
+// pass checks that shape (and the bounds every store below relies on).
+namespace abea {
+
+__global__ void __launch_bounds__(128) abea_postalign_kernel(PostalignArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int ri = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (ri >= a.n_reads) return;  // whole warps
+    const ReadDesc r = a.reads[ri];
+    int n = r.skip ? 0 : a.n_pairs[ri];
+    if (n < 0) n = 0;  // a read that ended with an error status has no pairs
+    const abea_aligned_pair_t* P = a.pairs + r.out_off;
+    bool ok = n <= r.out_cap;
+    for (int i = lane; ok && i < n; i += 32) {
+        const abea_aligned_pair_t p = P[i];
+        if (p.ref_pos < 0 || p.ref_pos >= r.n_kmers || p.read_pos < 0 || p.read_pos >= r.n_events) {
+            ok = false;
+        } else if (i > 0) {
+            const abea_aligned_pair_t q = P[i - 1];
+            const int dk = p.ref_pos - q.ref_pos, de = p.read_pos - q.read_pos;
+            ok = dk >= 0 && dk <= 1 && de >= 0 && de <= 1 && (dk | de) != 0;
+        }
+    }
+    ok = __all_sync(kFull, ok);
+    if (!ok || n == 0) {
+        if (lane == 0) {
+            a.count[ri] = ok ? 0 : ABEA_ERR_INTERNAL;
+            a.epb[ri] = 0.0;
+        }
+        return;
+    }
+    const int e_first = P[0].read_pos, e_last = P[n - 1].read_pos;
+    const char* s = a.seq + r.seq_off;
+    abea_index_pair_t* map = a.map + r.seq_off;
+    uint4* rec = reinterpret_cast<uint4*>(a.rec + r.ev_src);
+    int carry_e = -1, carry_k = -1, carry_rank = -1;  // the previous pair's event; the previous counting pair
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        const bool valid = i < n;
+        int k = -1, e = -1;
+        if (valid) {
+            const abea_aligned_pair_t p = P[i];
+            k = p.ref_pos;
+            e = p.read_pos;
+        }
+        int e_prev = __shfl_up_sync(kFull, e, 1);
+        if (lane == 0) e_prev = carry_e;
+        const bool q = valid && e != e_prev;
+        uint32_t b[ABEA_KMER_SIZE] = {};
+        int rank = 0;
+        if (q) {
+#pragma unroll
+            for (int j = 0; j < ABEA_KMER_SIZE; ++j) {
+                b[j] = (uint8_t)s[k + j];
+                rank = (rank << 2) | (int)base_rank(s[k + j]);
+            }
+        }
+        const unsigned qm = __ballot_sync(kFull, q);
+        const unsigned below = qm & ((1u << lane) - 1u);
+        const unsigned above = qm & ~((2u << lane) - 1u);  // lane 31: 2u << 31 wraps to 0, so none above
+        const int src = below ? 31 - __clz(below) : lane;
+        const int dst = above ? __ffs(above) - 1 : lane;
+        const int k_below = __shfl_sync(kFull, k, src);
+        const int rank_below = __shfl_sync(kFull, rank, src);
+        const int k_above = __shfl_sync(kFull, k, dst);
+        if (q) {
+            const int pk = below ? k_below : carry_k;
+            const int pr = below ? rank_below : carry_rank;
+            if (pk != k) map[k].start = e;                  // first counting pair of this k-mer
+            if (!above || k_above != k) map[k].stop = e;    // last one in this chunk; later chunks overwrite
+            const uint32_t hmm = rank != pr ? 'M' : 'E';
+            // the 32-byte event_alignment_t: ref_kmer[7] + pad, ref_position, read_idx,
+            // event_idx, rc, model_kmer[7], hmm_state, pad (little-endian bytes)
+            const uint4 lo = make_uint4(b[0] | b[1] << 8 | b[2] << 16 | b[3] << 24, b[4] | b[5] << 8, (uint32_t)k,
+                                        (uint32_t)ri);
+            const uint4 hi = make_uint4((uint32_t)e, b[0] << 8 | b[1] << 16 | b[2] << 24, b[3] | b[4] << 8 | b[5] << 16,
+                                        hmm);
+            rec[2 * (e - e_first)] = lo;
+            rec[2 * (e - e_first) + 1] = hi;
+        }
+        const int last = min(31, n - 1 - base);
+        carry_e = __shfl_sync(kFull, e, last);
+        if (qm) {
+            const int lq = 31 - __clz(qm);
+            carry_k = __shfl_sync(kFull, k, lq);
+            carry_rank = __shfl_sync(kFull, rank, lq);
+        }
+        __syncwarp();  // orders this chunk's map stores before the next chunk's
+    }
+    if (lane == 0) {
+        a.count[ri] = e_last - e_first + 1;
+        a.epb[ri] = (double)(e_last - e_first) / r.n_kmers;
+    }
+}
+
+cudaError_t launch_postalign(const PostalignArgs& a, cudaStream_t stream) {
+    if (a.n_reads > 0) abea_postalign_kernel<<<(a.n_reads + 3) / 4, 128, 0, stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace abea

@@ -105,6 +105,21 @@ struct MomArgs {
 // Method-of-moments scalings, one warp per read.
 cudaError_t launch_mom(const MomArgs& a, cudaStream_t stream);
 
+struct PostalignArgs {
+    const ReadDesc* reads;
+    int n_reads;
+    const char* seq;
+    const abea_aligned_pair_t* pairs;  // the run's AlignedPairs (2*event_ptr per read)
+    const int32_t* n_pairs;
+    abea_index_pair_t* map;            // [seq bytes], preset to {-1, -1}; read i from seq_off
+    abea_event_alignment_t* rec;       // [events], preset to 0; read i from ev_src (32-byte aligned)
+    double* epb;                       // [n] events per base
+    int32_t* count;                    // [n] records, or ABEA_ERR_INTERNAL for a malformed path
+};
+
+// f5c's postalign over a finished run's AlignedPairs, one warp per read.
+cudaError_t launch_postalign(const PostalignArgs& a, cudaStream_t stream);
+
 struct LaunchArgs {
     PreArgs pre;
     CoreArgs core;

@@ -1,4 +1,4 @@
-"""NumPy mirrors of the reference's shared C types (GPU/f5c.h:113-181) and the
+"""NumPy mirrors of the reference's shared C types (GPU/f5c.h:113-207) and the
 flattened batch layout of align_ocl() (GPU/align_cuda.c:432-497)."""
 from __future__ import annotations
 
@@ -23,8 +23,20 @@ PAIR_DTYPE = np.dtype([("ref_pos", "<i4"), ("read_pos", "<i4")])
 # EventKmerPair (8 B).
 EKPAIR_DTYPE = np.dtype([("event_idx", "<i4"), ("kmer_idx", "<i4")])
 
+# index_pair_t (8 B) and event_alignment_t (32 B), the outputs of f5c's postalign
+# (GPU/f5c.h:184-207): char ref_kmer[7]; i32 ref_position, read_idx, event_idx;
+# bool rc; char model_kmer[7]; char hmm_state.
+INDEX_PAIR_DTYPE = np.dtype([("start", "<i4"), ("stop", "<i4")])
+EVENT_ALIGNMENT_DTYPE = np.dtype({
+    "names": ["ref_kmer", "ref_position", "read_idx", "event_idx", "rc", "model_kmer", "hmm_state"],
+    "formats": ["S7", "<i4", "<i4", "<i4", "u1", "S7", "S1"],
+    "offsets": [0, 8, 12, 16, 20, 21, 28],
+    "itemsize": 32,
+})
+
 assert EVENT_DTYPE.itemsize == 24 and MODEL_DTYPE.itemsize == 12
 assert SCALINGS_DTYPE.itemsize == 16 and PAIR_DTYPE.itemsize == 8
+assert INDEX_PAIR_DTYPE.itemsize == 8 and EVENT_ALIGNMENT_DTYPE.itemsize == 32
 
 
 def n_kmers_of(read_len):
@@ -122,6 +134,18 @@ def from_reads(seqs, event_arrays, scalings, model, meta=None) -> Batch:
         model=np.ascontiguousarray(np.asarray(model, dtype=MODEL_DTYPE)),
         meta=dict(meta or {}),
     )
+
+
+def split_postalign(batch: Batch, out: dict):
+    """Per-read (records, base_to_event_map) of a postalign result: read i's
+    n_alignment[i] records from event_ptr[i] and its n_kmers map entries from
+    read_ptr[i]."""
+    res = []
+    for i in range(batch.n_reads):
+        e, c = int(batch.event_ptr[i]), max(int(out["n_alignment"][i]), 0)
+        p, nk = int(batch.read_ptr[i]), max(int(batch.read_len[i]) - KMER_SIZE + 1, 0)
+        res.append((out["alignment"][e : e + c].copy(), out["base_to_event_map"][p : p + nk].copy()))
+    return res
 
 
 def split_pairs(batch: Batch, pairs: np.ndarray, counts: np.ndarray):

@@ -18,6 +18,8 @@
  *   abea_scalings_t     == scalings_t     (16 B, CACHED_LOG layout)
  *   abea_aligned_pair_t == AlignedPair    (8 B)
  *   abea_event_kmer_pair_t == EventKmerPair (8 B)
+ *   abea_index_pair_t   == index_pair_t   (8 B)
+ *   abea_event_alignment_t == event_alignment_t (32 B)
  */
 #ifndef ABEA_H
 #define ABEA_H
@@ -34,7 +36,7 @@ extern "C" {
 #define ABEA_NUM_KMER 4096
 #define ABEA_BANDWIDTH 100
 
-/* ---- shared types (GPU/f5c.h:113-181) ---------------------------------- */
+/* ---- shared types (GPU/f5c.h:113-207) ---------------------------------- */
 typedef struct {
     uint64_t start;
     float length;
@@ -72,6 +74,24 @@ typedef struct {
     int32_t kmer_idx;
 } abea_event_kmer_pair_t;
 
+/* Outputs of f5c's postalign (GPU/f5cmisc.h:51-52): index_pair_t and
+ * event_alignment_t (GPU/f5c.h:184-207).  `rc` is the reference's `bool`
+ * (one byte); the 32-byte layout is the same. */
+typedef struct {
+    int32_t start;
+    int32_t stop; /* inclusive */
+} abea_index_pair_t;
+
+typedef struct {
+    char ref_kmer[ABEA_KMER_SIZE + 1];
+    int32_t ref_position;
+    int32_t read_idx;
+    int32_t event_idx;
+    uint8_t rc;
+    char model_kmer[ABEA_KMER_SIZE + 1];
+    char hmm_state;
+} abea_event_alignment_t;
+
 /* ---- status codes ------------------------------------------------------ */
 typedef enum {
     ABEA_OK = 0,
@@ -101,8 +121,8 @@ typedef enum { ABEA_MODE_PLAIN = 0, ABEA_MODE_BATCHED = 1 } abea_mode_t;
 typedef enum {
     ABEA_OPT_MODE = 0,          /* abea_mode_t */
     ABEA_OPT_STORE_SCORES = 1,  /* 1: keep every band's scores in HBM (reference layout, GPU/align_cuda.c:573-577) */
-    ABEA_OPT_USE_GRAPH = 2,     /* BATCHED only: 1 = replay the three stages as one CUDA graph */
-    ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide (4-warp) shape; 0 = autotuned */
+    ABEA_OPT_USE_GRAPH = 2,     /* BATCHED only: 1 = replay the step as one CUDA graph */
+    ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide (16-warp) shape; 0 = autotuned */
     ABEA_OPT_SPIN_LIMIT = 4,    /* upper bound on any device-side wait, in polling iterations */
     ABEA_OPT_VAR_AWARE = 5,     /* 1: emissions use level_stdv*var and level_log_stdv+log_var (the
                                    reference ignores var, GPU/align_cuda.cl:509); taken at batch creation */
@@ -316,6 +336,27 @@ abea_status_t abea_batch_recalibrate(abea_ctx_t *ctx, abea_batch_t *batch, int32
  * them the batch's scalings for the next run. */
 abea_status_t abea_batch_estimate_scalings(abea_ctx_t *ctx, abea_batch_t *batch, abea_scalings_t *out,
                                            int32_t apply);
+
+/* f5c's postalign (GPU/f5cmisc.h:51-52, prototype only in the reference) for
+ * every read of a batch after abea_batch_run, on the AlignedPairs in HBM:
+ *   base_to_event_map[read_ptr[i] + k], k < n_kmers: the first and last event
+ *       aligned to k-mer k, counting a pair only when its event differs from
+ *       the previous pair's; {-1, -1} for a k-mer with none.  Entries past
+ *       n_kmers of each read are {-1, -1}.  Size: the batch's read buffer
+ *       (max read_ptr[i] + read_len[i] + 1 entries).
+ *   alignment[event_ptr[i] + j], j < n_alignment[i]: for every k-mer k in
+ *       order and every event of its range, {ref_kmer = model_kmer = the six
+ *       bases at k, ref_position = k, read_idx = i, event_idx, rc = 0,
+ *       hmm_state = 'M' when the k-mer's rank differs from the previous
+ *       record's, else 'E'}.  Size: max event_ptr[i] + n_events[i] records.
+ *   events_per_base[i] = (last event - first event on the path) / n_kmers.
+ *   n_alignment[i]: the record count (at most n_events[i]); 0 with
+ *       events_per_base 0 for a read without AlignedPairs (failed quality
+ *       checks, nothing to align).
+ * Any output pointer may be NULL. */
+abea_status_t abea_batch_postalign(abea_ctx_t *ctx, abea_batch_t *batch, abea_event_alignment_t *alignment,
+                                   abea_index_pair_t *base_to_event_map, double *events_per_base,
+                                   int32_t *n_alignment);
 
 /* ---- serving stream (no counterpart in the reference) --------------------
  * A stream of reads in the batch layout of abea_align_batch, admitted in input

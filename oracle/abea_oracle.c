@@ -595,3 +595,57 @@ void oracle_mom(const char *seq, int32_t seq_len, const abea_event_t *events, in
     *scale = sqrt(ev / kv);
     *shift = em - *scale * km;
 }
+
+/* ---- postalign (no body in the reference) ----
+ * f5c's postalign is only a prototype in the reference (GPU/f5cmisc.h:51-52;
+ * its output types index_pair_t and event_alignment_t are GPU/f5c.h:184-207).
+ * Restated as two serial loops, for any array of pairs: (1) over the pairs in
+ * order, a pair whose event differs from the previous pair's sets its k-mer's
+ * map start (when still -1) and stop; (2) over the k-mers in order, one record
+ * for every event of each k-mer's range, 'M' when the k-mer's rank differs
+ * from the previous record's, else 'E'.  events_per_base = (largest event -
+ * smallest event) / n_kmers; 0 with no pairs.  Returns the record count,
+ * ABEA_ERR_CAPACITY past out_cap, ABEA_ERR_INVALID_ARG for a pair outside the
+ * read. */
+int32_t oracle_postalign(abea_event_alignment_t *out, int32_t out_cap, abea_index_pair_t *map,
+                         double *events_per_base, const char *seq, int32_t n_kmers,
+                         const abea_aligned_pair_t *pairs, int32_t n_pairs, int32_t read_idx) {
+    for (int32_t k = 0; k < n_kmers; ++k) {
+        map[k].start = -1;
+        map[k].stop = -1;
+    }
+    *events_per_base = 0.0;
+    if (n_pairs <= 0) return 0;
+    int32_t lo = INT32_MAX, hi = INT32_MIN, prev_event = -1;
+    for (int32_t i = 0; i < n_pairs; ++i) {
+        const int32_t k = pairs[i].ref_pos, e = pairs[i].read_pos;
+        if (k < 0 || k >= n_kmers || e < 0) return ABEA_ERR_INVALID_ARG;
+        if (e != prev_event) {
+            if (map[k].start == -1) map[k].start = e;
+            map[k].stop = e;
+        }
+        if (e < lo) lo = e;
+        if (e > hi) hi = e;
+        prev_event = e;
+    }
+    *events_per_base = (double)(hi - lo) / n_kmers;
+    int32_t n = 0, prev_rank = -1;
+    for (int32_t k = 0; k < n_kmers; ++k) {
+        if (map[k].start == -1) continue;
+        const int32_t rank = (int32_t)oracle_kmer_rank(seq + k);
+        for (int32_t e = map[k].start; e <= map[k].stop; ++e) {
+            if (n >= out_cap) return ABEA_ERR_CAPACITY;
+            abea_event_alignment_t *a = &out[n++];
+            memset(a, 0, sizeof(*a));
+            memcpy(a->ref_kmer, seq + k, ABEA_KMER_SIZE);
+            memcpy(a->model_kmer, seq + k, ABEA_KMER_SIZE);
+            a->ref_position = k;
+            a->read_idx = read_idx;
+            a->event_idx = e;
+            a->rc = 0;
+            a->hmm_state = rank != prev_rank ? 'M' : 'E';
+            prev_rank = rank;
+        }
+    }
+    return n;
+}

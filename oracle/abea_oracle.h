@@ -103,6 +103,13 @@ uint32_t oracle_kmer_rank(const char *s);
 /* The double-rounded cell sum of the reference, (float)(((double)a + b) + (double)c). */
 float oracle_add3(float a, double b, float c);
 
+/* f5c's postalign restated (prototype only in the reference, GPU/f5cmisc.h:51-52):
+ * map[n_kmers] and out[<= out_cap] from one read's AlignedPairs.  Returns the
+ * record count, ABEA_ERR_CAPACITY or ABEA_ERR_INVALID_ARG. */
+int32_t oracle_postalign(abea_event_alignment_t *out, int32_t out_cap, abea_index_pair_t *map,
+                         double *events_per_base, const char *seq, int32_t n_kmers,
+                         const abea_aligned_pair_t *pairs, int32_t n_pairs, int32_t read_idx);
+
 #ifdef __cplusplus
 }
 #endif

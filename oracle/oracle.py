@@ -25,6 +25,13 @@ MODEL_DTYPE = np.dtype([("level_mean", "<f4"), ("level_stdv", "<f4"), ("level_lo
 SCALINGS_DTYPE = np.dtype([("scale", "<f4"), ("shift", "<f4"), ("var", "<f4"), ("log_var", "<f4")])
 PAIR_DTYPE = np.dtype([("ref_pos", "<i4"), ("read_pos", "<i4")])
 EKPAIR_DTYPE = np.dtype([("event_idx", "<i4"), ("kmer_idx", "<i4")])
+INDEX_PAIR_DTYPE = np.dtype([("start", "<i4"), ("stop", "<i4")])
+EVENT_ALIGNMENT_DTYPE = np.dtype({
+    "names": ["ref_kmer", "ref_position", "read_idx", "event_idx", "rc", "model_kmer", "hmm_state"],
+    "formats": ["S7", "<i4", "<i4", "<i4", "u1", "S7", "S1"],
+    "offsets": [0, 8, 12, 16, 20, 21, 28],
+    "itemsize": 32,
+})
 
 
 class _Scalings(C.Structure):
@@ -74,6 +81,9 @@ def lib():
         L.oracle_mom.restype = None
         L.oracle_mom.argtypes = [C.c_char_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
                                  C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.oracle_postalign.restype = C.c_int32
+        L.oracle_postalign.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_double), C.c_char_p,
+                                       C.c_int32, C.c_void_p, C.c_int32, C.c_int32]
         L.oracle_n_bands.restype = C.c_int64
         L.oracle_n_bands.argtypes = [C.c_int32, C.c_int32]
         _lib = L
@@ -179,6 +189,43 @@ def mom(seq: bytes, events, model):
     sc, sh = C.c_double(), C.c_double()
     lib().oracle_mom(bytes(seq), len(seq), _ptr(events), len(events), _ptr(model), C.byref(sc), C.byref(sh))
     return sc.value, sh.value
+
+
+def postalign(seq: bytes, pairs, read_idx: int = 0, out_cap: int | None = None):
+    """f5c's postalign of one read's AlignedPairs: (records, base_to_event_map,
+    events_per_base, status); status is the record count or a negative code."""
+    pairs = np.asarray(pairs)
+    if pairs.dtype != PAIR_DTYPE:  # an [n, 2] integer array of (ref_pos, read_pos)
+        pairs = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2).view(PAIR_DTYPE).reshape(-1)
+    pairs = np.ascontiguousarray(pairs)
+    nk = max(len(seq) - 5, 0)
+    cap = len(pairs) if out_cap is None else out_cap
+    rec = np.zeros(max(cap, 1), dtype=EVENT_ALIGNMENT_DTYPE)
+    bmap = np.zeros(max(nk, 1), dtype=INDEX_PAIR_DTYPE)
+    epb = C.c_double()
+    n = lib().oracle_postalign(_ptr(rec), cap, _ptr(bmap), C.byref(epb), bytes(seq), nk, _ptr(pairs), len(pairs),
+                               int(read_idx))
+    return rec[: max(n, 0)], bmap[:nk], epb.value, n
+
+
+def postalign_batch(batch, pairs, counts):
+    """postalign over a batch's flattened AlignedPairs, in the layout of
+    abea_batch_postalign: (records [events], map [read buffer], events_per_base,
+    n_alignment)."""
+    n = batch.n_reads
+    n_rec = int((batch.event_ptr + batch.n_events).max()) if n else 0
+    n_map = int((batch.read_ptr + batch.read_len + 1).max()) if n else 0
+    rec = np.zeros(n_rec, dtype=EVENT_ALIGNMENT_DTYPE)
+    bmap = np.full(n_map, -1, dtype=INDEX_PAIR_DTYPE)
+    epb = np.zeros(n)
+    cnt = np.zeros(n, dtype=np.int32)
+    for i in range(n):
+        e, c, p = int(batch.event_ptr[i]), max(int(counts[i]), 0), int(batch.read_ptr[i])
+        seq = batch.read[p : p + int(batch.read_len[i])].tobytes()
+        r, m, epb[i], cnt[i] = postalign(seq, pairs[2 * e : 2 * e + c], i, out_cap=int(batch.n_events[i]))
+        rec[e : e + len(r)] = r
+        bmap[p : p + len(m)] = m
+    return rec, bmap, epb, cnt
 
 
 def add3(a: float, b: float, c: float) -> float:
