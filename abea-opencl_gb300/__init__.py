@@ -266,13 +266,13 @@ class DeviceBatch:
     def postalign(self):
         """f5c's postalign for every read of the last run (abea_batch_postalign):
         dict with alignment [events] (EVENT_ALIGNMENT_DTYPE, read i's records from
-        event_ptr[i]), base_to_event_map [read buffer] (INDEX_PAIR_DTYPE, read i's
+        event_ptr[i]), base_to_event_map [max(read_ptr + read_len)] (INDEX_PAIR_DTYPE, read i's
         n_kmers entries from read_ptr[i]), events_per_base [n] and n_alignment [n];
         `split_postalign` cuts them per read."""
         b = self.batch
         n = b.n_reads
         n_rec = int((b.event_ptr + b.n_events).max()) if n else 0
-        n_map = int((b.read_ptr + b.read_len + 1).max()) if n else 0
+        n_map = int((b.read_ptr + b.read_len).max()) if n else 0
         rec = np.zeros(max(n_rec, 1), dtype=EVENT_ALIGNMENT_DTYPE)
         bmap = np.zeros(max(n_map, 1), dtype=INDEX_PAIR_DTYPE)
         epb = np.zeros(max(n, 1))

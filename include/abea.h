@@ -342,8 +342,8 @@ abea_status_t abea_batch_estimate_scalings(abea_ctx_t *ctx, abea_batch_t *batch,
  *   base_to_event_map[read_ptr[i] + k], k < n_kmers: the first and last event
  *       aligned to k-mer k, counting a pair only when its event differs from
  *       the previous pair's; {-1, -1} for a k-mer with none.  Entries past
- *       n_kmers of each read are {-1, -1}.  Size: the batch's read buffer
- *       (max read_ptr[i] + read_len[i] + 1 entries).
+ *       n_kmers of each read are {-1, -1}.  Size: max(read_ptr[i] +
+ *       read_len[i]) entries.
  *   alignment[event_ptr[i] + j], j < n_alignment[i]: for every k-mer k in
  *       order and every event of its range, {ref_kmer = model_kmer = the six
  *       bases at k, ref_position = k, read_idx = i, event_idx, rc = 0,

@@ -210,11 +210,11 @@ def postalign(seq: bytes, pairs, read_idx: int = 0, out_cap: int | None = None):
 
 def postalign_batch(batch, pairs, counts):
     """postalign over a batch's flattened AlignedPairs, in the layout of
-    abea_batch_postalign: (records [events], map [read buffer], events_per_base,
+    abea_batch_postalign: (records [events], map [max(read_ptr + read_len)], events_per_base,
     n_alignment)."""
     n = batch.n_reads
     n_rec = int((batch.event_ptr + batch.n_events).max()) if n else 0
-    n_map = int((batch.read_ptr + batch.read_len + 1).max()) if n else 0
+    n_map = int((batch.read_ptr + batch.read_len).max()) if n else 0
     rec = np.zeros(n_rec, dtype=EVENT_ALIGNMENT_DTYPE)
     bmap = np.full(n_map, -1, dtype=INDEX_PAIR_DTYPE)
     epb = np.zeros(n)
