@@ -263,21 +263,24 @@ class DeviceBatch:
         _check(lib().abea_batch_estimate_scalings(self.ctx.h, self.h, _p(out), 1 if apply else 0))
         return out[: self.batch.n_reads]
 
-    def postalign(self):
+    def postalign(self, outputs: bool = True):
         """f5c's postalign for every read of the last run (abea_batch_postalign):
         dict with alignment [events] (EVENT_ALIGNMENT_DTYPE, read i's records from
         event_ptr[i]), base_to_event_map [max(read_ptr + read_len)] (INDEX_PAIR_DTYPE, read i's
         n_kmers entries from read_ptr[i]), events_per_base [n] and n_alignment [n];
-        `split_postalign` cuts them per read."""
+        `split_postalign` cuts them per read.  outputs=False leaves the records, maps
+        and events per base on the device (None here) and returns only the counts."""
         b = self.batch
         n = b.n_reads
         n_rec = int((b.event_ptr + b.n_events).max()) if n else 0
         n_map = int((b.read_ptr + b.read_len).max()) if n else 0
-        rec = np.zeros(max(n_rec, 1), dtype=EVENT_ALIGNMENT_DTYPE)
-        bmap = np.zeros(max(n_map, 1), dtype=INDEX_PAIR_DTYPE)
-        epb = np.zeros(max(n, 1))
+        rec = np.zeros(max(n_rec, 1), dtype=EVENT_ALIGNMENT_DTYPE) if outputs else None
+        bmap = np.zeros(max(n_map, 1), dtype=INDEX_PAIR_DTYPE) if outputs else None
+        epb = np.zeros(max(n, 1)) if outputs else None
         cnt = np.zeros(max(n, 1), dtype=np.int32)
         _check(lib().abea_batch_postalign(self.ctx.h, self.h, _p(rec), _p(bmap), _p(epb), _p(cnt)))
+        if not outputs:
+            return dict(alignment=None, base_to_event_map=None, events_per_base=None, n_alignment=cnt[:n])
         return dict(alignment=rec[:n_rec], base_to_event_map=bmap[:n_map], events_per_base=epb[:n],
                     n_alignment=cnt[:n])
 

@@ -2381,6 +2381,8 @@ cudaError_t launch_mom(const MomArgs& a, cudaStream_t stream) {
 // pass checks that shape (and the bounds every store below relies on).
 namespace abea {
 
+constexpr int kPaUnroll = 8;  // chunks of 32 pairs whose loads are in flight together
+
 __global__ void __launch_bounds__(128) abea_postalign_kernel(PostalignArgs a) {
     const int lane = threadIdx.x & 31;
     const int ri = blockIdx.x * 4 + (threadIdx.x >> 5);
@@ -2390,14 +2392,41 @@ __global__ void __launch_bounds__(128) abea_postalign_kernel(PostalignArgs a) {
     if (n < 0) n = 0;  // a read that ended with an error status has no pairs
     const abea_aligned_pair_t* P = a.pairs + r.out_off;
     bool ok = n <= r.out_cap;
-    for (int i = lane; ok && i < n; i += 32) {
-        const abea_aligned_pair_t p = P[i];
-        if (p.ref_pos < 0 || p.ref_pos >= r.n_kmers || p.read_pos < 0 || p.read_pos >= r.n_events) {
-            ok = false;
-        } else if (i > 0) {
-            const abea_aligned_pair_t q = P[i - 1];
-            const int dk = p.ref_pos - q.ref_pos, de = p.read_pos - q.read_pos;
-            ok = dk >= 0 && dk <= 1 && de >= 0 && de <= 1 && (dk | de) != 0;
+    // pass 1: bounds and unit steps; pair i-1 of lane 0 is lane 31 of the previous chunk
+    if (__all_sync(kFull, ok)) {
+        int k31 = -1, e31 = -1;
+        for (int base = 0; base < n; base += 32 * kPaUnroll) {
+            int kk[kPaUnroll], ee[kPaUnroll];
+#pragma unroll
+            for (int u = 0; u < kPaUnroll; ++u) {
+                const int i = base + 32 * u + lane;
+                kk[u] = -1;
+                ee[u] = -1;
+                if (i < n) {
+                    const abea_aligned_pair_t p = P[i];
+                    kk[u] = p.ref_pos;
+                    ee[u] = p.read_pos;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kPaUnroll; ++u) {
+                const int i = base + 32 * u + lane;
+                int qk = __shfl_up_sync(kFull, kk[u], 1), qe = __shfl_up_sync(kFull, ee[u], 1);
+                if (lane == 0) {
+                    qk = k31;
+                    qe = e31;
+                }
+                if (i < n) {
+                    if (kk[u] < 0 || kk[u] >= r.n_kmers || ee[u] < 0 || ee[u] >= r.n_events) {
+                        ok = false;
+                    } else if (i > 0) {
+                        const int dk = kk[u] - qk, de = ee[u] - qe;
+                        ok = ok && dk >= 0 && dk <= 1 && de >= 0 && de <= 1 && (dk | de) != 0;
+                    }
+                }
+                k31 = __shfl_sync(kFull, kk[u], 31);
+                e31 = __shfl_sync(kFull, ee[u], 31);
+            }
         }
     }
     ok = __all_sync(kFull, ok);
@@ -2413,58 +2442,74 @@ __global__ void __launch_bounds__(128) abea_postalign_kernel(PostalignArgs a) {
     abea_index_pair_t* map = a.map + r.seq_off;
     uint4* rec = reinterpret_cast<uint4*>(a.rec + r.ev_src);
     int carry_e = -1, carry_k = -1, carry_rank = -1;  // the previous pair's event; the previous counting pair
-    for (int base = 0; base < n; base += 32) {
-        const int i = base + lane;
-        const bool valid = i < n;
-        int k = -1, e = -1;
-        if (valid) {
-            const abea_aligned_pair_t p = P[i];
-            k = p.ref_pos;
-            e = p.read_pos;
-        }
-        int e_prev = __shfl_up_sync(kFull, e, 1);
-        if (lane == 0) e_prev = carry_e;
-        const bool q = valid && e != e_prev;
-        uint32_t b[ABEA_KMER_SIZE] = {};
-        int rank = 0;
-        if (q) {
+    for (int base = 0; base < n; base += 32 * kPaUnroll) {
+        int kk[kPaUnroll], ee[kPaUnroll];
 #pragma unroll
-            for (int j = 0; j < ABEA_KMER_SIZE; ++j) {
-                b[j] = (uint8_t)s[k + j];
-                rank = (rank << 2) | (int)base_rank(s[k + j]);
+        for (int u = 0; u < kPaUnroll; ++u) {
+            const int i = base + 32 * u + lane;
+            kk[u] = -1;
+            ee[u] = -1;
+            if (i < n) {
+                const abea_aligned_pair_t p = P[i];
+                kk[u] = p.ref_pos;
+                ee[u] = p.read_pos;
             }
         }
-        const unsigned qm = __ballot_sync(kFull, q);
-        const unsigned below = qm & ((1u << lane) - 1u);
-        const unsigned above = qm & ~((2u << lane) - 1u);  // lane 31: 2u << 31 wraps to 0, so none above
-        const int src = below ? 31 - __clz(below) : lane;
-        const int dst = above ? __ffs(above) - 1 : lane;
-        const int k_below = __shfl_sync(kFull, k, src);
-        const int rank_below = __shfl_sync(kFull, rank, src);
-        const int k_above = __shfl_sync(kFull, k, dst);
-        if (q) {
-            const int pk = below ? k_below : carry_k;
-            const int pr = below ? rank_below : carry_rank;
-            if (pk != k) map[k].start = e;                  // first counting pair of this k-mer
-            if (!above || k_above != k) map[k].stop = e;    // last one in this chunk; later chunks overwrite
-            const uint32_t hmm = rank != pr ? 'M' : 'E';
-            // the 32-byte event_alignment_t: ref_kmer[7] + pad, ref_position, read_idx,
-            // event_idx, rc, model_kmer[7], hmm_state, pad (little-endian bytes)
-            const uint4 lo = make_uint4(b[0] | b[1] << 8 | b[2] << 16 | b[3] << 24, b[4] | b[5] << 8, (uint32_t)k,
-                                        (uint32_t)ri);
-            const uint4 hi = make_uint4((uint32_t)e, b[0] << 8 | b[1] << 16 | b[2] << 24, b[3] | b[4] << 8 | b[5] << 16,
-                                        hmm);
-            rec[2 * (e - e_first)] = lo;
-            rec[2 * (e - e_first) + 1] = hi;
+        // counting pairs (event differs from the previous pair's) and their k-mers' bases
+        bool qq[kPaUnroll];
+        uint32_t w0[kPaUnroll], w1[kPaUnroll];  // bases 0-3 and 4-5 of the k-mer, little-endian
+#pragma unroll
+        for (int u = 0; u < kPaUnroll; ++u) {
+            int e_prev = __shfl_up_sync(kFull, ee[u], 1);
+            if (lane == 0) e_prev = carry_e;
+            qq[u] = base + 32 * u + lane < n && ee[u] != e_prev;
+            carry_e = __shfl_sync(kFull, ee[u], 31);
+            w0[u] = 0;
+            w1[u] = 0;
+            if (qq[u]) {
+                const uint8_t* sb = reinterpret_cast<const uint8_t*>(s + kk[u]);
+                w0[u] = (uint32_t)sb[0] | (uint32_t)sb[1] << 8 | (uint32_t)sb[2] << 16 | (uint32_t)sb[3] << 24;
+                w1[u] = (uint32_t)sb[4] | (uint32_t)sb[5] << 8;
+            }
         }
-        const int last = min(31, n - 1 - base);
-        carry_e = __shfl_sync(kFull, e, last);
-        if (qm) {
-            const int lq = 31 - __clz(qm);
-            carry_k = __shfl_sync(kFull, k, lq);
-            carry_rank = __shfl_sync(kFull, rank, lq);
+#pragma unroll
+        for (int u = 0; u < kPaUnroll; ++u) {
+            const int k = kk[u], e = ee[u];
+            const bool q = qq[u];
+            int rank = 0;
+            if (q) {
+#pragma unroll
+                for (int j = 0; j < ABEA_KMER_SIZE; ++j)
+                    rank = (rank << 2) | (int)base_rank((char)((j < 4 ? w0[u] >> (8 * j) : w1[u] >> (8 * (j - 4))) & 0xff));
+            }
+            const unsigned qm = __ballot_sync(kFull, q);
+            const unsigned below = qm & ((1u << lane) - 1u);
+            const unsigned above = qm & ~((2u << lane) - 1u);  // lane 31: 2u << 31 wraps to 0, so none above
+            const int src = below ? 31 - __clz(below) : lane;
+            const int dst = above ? __ffs(above) - 1 : lane;
+            const int k_below = __shfl_sync(kFull, k, src);
+            const int rank_below = __shfl_sync(kFull, rank, src);
+            const int k_above = __shfl_sync(kFull, k, dst);
+            if (q) {
+                const int pk = below ? k_below : carry_k;
+                const int pr = below ? rank_below : carry_rank;
+                if (pk != k) map[k].start = e;                // first counting pair of this k-mer
+                if (!above || k_above != k) map[k].stop = e;  // last one in this chunk; later chunks overwrite
+                const uint32_t hmm = rank != pr ? 'M' : 'E';
+                // the 32-byte event_alignment_t: ref_kmer[7] + pad, ref_position, read_idx,
+                // event_idx, rc, model_kmer[7], hmm_state, pad (little-endian bytes)
+                const uint4 lo = make_uint4(w0[u], w1[u], (uint32_t)k, (uint32_t)ri);
+                const uint4 hi = make_uint4((uint32_t)e, w0[u] << 8, w0[u] >> 24 | w1[u] << 8, hmm);
+                rec[2 * (e - e_first)] = lo;
+                rec[2 * (e - e_first) + 1] = hi;
+            }
+            if (qm) {
+                const int lq = 31 - __clz(qm);
+                carry_k = __shfl_sync(kFull, k, lq);
+                carry_rank = __shfl_sync(kFull, rank, lq);
+            }
+            __syncwarp();  // orders this chunk's map stores before the next chunk's
         }
-        __syncwarp();  // orders this chunk's map stores before the next chunk's
     }
     if (lane == 0) {
         a.count[ri] = e_last - e_first + 1;

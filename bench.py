@@ -331,6 +331,65 @@ def adjoint_report(pkg, synth, device, seed):
     }
 
 
+def next_rows_report(pkg, synth, device, seed, cpu: bool):
+    """The rows after the path, on the f5c batch after one batched run: f5c's
+    postalign (abea_batch_postalign) and the method-of-moments scalings
+    (abea_batch_estimate_scalings).  Device time by CUDA events on the library's
+    stream around the entry (memsets, kernel, the per-read counts or scalings
+    back to the host); end to end = wall time with every output copied to
+    (pageable) host arrays; the oracle's single-thread loops beside them."""
+    b = synth.make_batch("f5c_batch", seed=seed)
+    ctx = pkg.Context(device, pkg.MODE_BATCHED)
+    dev = ctx.upload(b)
+    dev.run()
+    pairs, counts = dev.results()
+    n_pairs = int(np.maximum(counts, 0).sum())
+    dev.postalign(outputs=False)
+    dt = []
+    for _ in range(5):
+        ctx.flush_l2()
+        ctx.mark(0)
+        got = dev.postalign(outputs=False)
+        ctx.mark(1)
+        dt.append(ctx.elapsed(0, 1))
+    t0 = time.perf_counter()
+    dev.postalign()
+    e2e = (time.perf_counter() - t0) * 1e3
+    n_rec = int(got["n_alignment"].sum())
+    n_kmers = int(np.maximum(b.read_len - 5, 0).sum())
+    # algorithmic bytes: every pair read once, every record and map entry written once
+    algo = 8 * n_pairs + 32 * n_rec + 8 * n_kmers
+    ms = min(dt)
+    peak, peak_kind = measured_peak_hbm()
+    pa = {"reads": b.n_reads, "pairs": n_pairs, "records": n_rec, "device_ms": ms, "device_ms_mean": statistics.mean(dt),
+          "e2e_ms_with_host_outputs": e2e, "algorithmic_bytes": algo,
+          "achieved_gbs": algo / (ms / 1e3) / 1e9, "peak_gbs": peak, "peak_kind": f"{peak_kind} (hbm_gbs)",
+          "note": "device_ms includes the two output memsets and the count copy; a step this small is launch-bound"}
+    dev.estimate_scalings()
+    mt = []
+    for _ in range(5):
+        ctx.mark(0)
+        dev.estimate_scalings()
+        ctx.mark(1)
+        mt.append(ctx.elapsed(0, 1))
+    mom = {"reads": b.n_reads, "device_ms": min(mt), "device_ms_mean": statistics.mean(mt)}
+    if cpu:
+        from oracle import oracle
+        t0 = time.perf_counter()
+        oracle.postalign_batch(b, pairs, counts)
+        pa["cpu_oracle_ms"] = (time.perf_counter() - t0) * 1e3
+        pa["cpu_oracle_cores"] = 1
+        t0 = time.perf_counter()
+        for i in range(b.n_reads):
+            p, e = int(b.read_ptr[i]), int(b.event_ptr[i])
+            oracle.mom(b.read[p:p + int(b.read_len[i])].tobytes(), b.events[e:e + int(b.n_events[i])], b.model)
+        mom["cpu_oracle_ms"] = (time.perf_counter() - t0) * 1e3
+        mom["cpu_oracle_cores"] = 1
+    dev.close()
+    ctx.close()
+    return {"postalign": pa, "method_of_moments": mom, "workload": "f5c_batch seed %d after one batched run" % seed}
+
+
 def serving_report(pkg, synth, device, seed, mbases: float):
     """The serving stream: `mbases` Mbases of reads (lognormal, median 8 kb, at
     most 200 kb) admitted in order into device batches by footprint, two in
@@ -510,6 +569,7 @@ def ours(args, dist):
         out["per_config"] = per
     if args.compare and dist.world == 1:
         out["adjoint"] = adjoint_report(pkg, synth, device, args.seed)
+        out["next_rows"] = next_rows_report(pkg, synth, device, args.seed, args.cpu)
     if args.compare and dist.world == 1 and args.serving_mbases > 0:
         out["serving"] = serving_report(pkg, synth, device, args.seed, args.serving_mbases)
     if args.cpu and dist.world == 1:
