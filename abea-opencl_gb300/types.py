@@ -144,7 +144,10 @@ def split_postalign(batch: Batch, out: dict):
     for i in range(batch.n_reads):
         e, c = int(batch.event_ptr[i]), max(int(out["n_alignment"][i]), 0)
         p, nk = int(batch.read_ptr[i]), max(int(batch.read_len[i]) - KMER_SIZE + 1, 0)
-        res.append((out["alignment"][e : e + c].copy(), out["base_to_event_map"][p : p + nk].copy()))
+        rec = out["alignment"][e : e + c]
+        # a byte copy: ndarray.copy() of a dtype with padding leaves the padding bytes unset
+        rec = rec.view(np.uint8).copy().view(rec.dtype)
+        res.append((rec, out["base_to_event_map"][p : p + nk].copy()))
     return res
 
 

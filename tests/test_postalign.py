@@ -190,3 +190,21 @@ def test_postalign_needs_a_run():
     with pytest.raises(abea.AbeaError):
         dev.postalign()
     ctx.close()
+
+
+def test_batch_layout_of_the_oracle_and_the_split_helper(oracle_mod):
+    """postalign_batch writes each read where abea_batch_postalign does (records
+    from event_ptr, map entries from read_ptr), and split_postalign cuts them
+    back into the per-read results."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("small", seed=4, lengths=[200, 700, 1300])
+    pairs, counts, _ = oracle_mod.align_batch(batch, threads=2)
+    rec, bmap, epb, cnt = oracle_mod.postalign_batch(batch, pairs, counts)
+    assert len(rec) == int((batch.event_ptr + batch.n_events).max())
+    assert len(bmap) == int((batch.read_ptr + batch.read_len).max())
+    out = dict(alignment=rec, base_to_event_map=bmap, events_per_base=epb, n_alignment=cnt)
+    for i, ((r, m), p) in enumerate(zip(abea.split_postalign(batch, out), abea.split_pairs(batch, pairs, counts))):
+        r1, m1, e1, n1 = oracle_mod.postalign(batch.sequence(i), p, i)
+        assert n1 == cnt[i] == len(r) and epb[i] == e1
+        assert np.array_equal(r.view(np.uint8), r1.view(np.uint8)) and np.array_equal(m, m1)
+        assert np.all(r["read_idx"] == i)
