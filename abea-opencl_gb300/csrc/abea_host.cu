@@ -19,6 +19,7 @@
 #include <new>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "abea_internal.h"
@@ -1233,6 +1234,75 @@ extern "C" abea_status_t abea_align_batch_persistent(abea_ctx_t* c, int32_t n_re
 
 // f5c's db_t arrays: flatten into pinned staging (GPU/align_cuda.c:432-497's layout),
 // align, unflatten.
+// Copies f5c's per-read arrays into the flattened layout (reads NUL separated
+// from read_ptr[i], events from event_ptr[i]).  Batches of at least
+// kStageMinBytes are split into contiguous ranges of reads of about equal bytes,
+// one per host thread (up to kStageThreads, or `threads` when positive).
+constexpr int kStageThreads = 8;
+constexpr int64_t kStageMinBytes = 8 << 20;
+static void stage_db(size_t n, char* const* read, const int32_t* read_len, const abea_event_table_t* et,
+                     const int64_t* read_ptr, const int64_t* event_ptr, char* seq, abea_event_t* ev,
+                     int64_t total_bytes, int threads) {
+    auto copy = [=](size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; ++i) {
+            if (read_len[i] > 0) memcpy(seq + read_ptr[i], read[i], (size_t)read_len[i]);
+            seq[read_ptr[i] + read_len[i]] = 0;
+            if (et[i].n > 0) memcpy(ev + event_ptr[i], et[i].event, sizeof(abea_event_t) * et[i].n);
+        }
+    };
+    int t = threads;
+    if (t <= 0) {
+        const unsigned hw = std::max(std::thread::hardware_concurrency(), 1u);
+        t = total_bytes < kStageMinBytes ? 1 : (int)std::min<unsigned>((unsigned)kStageThreads, hw);
+    }
+    if (t <= 1 || n < 2 || total_bytes <= 0) {
+        copy(0, n);
+        return;
+    }
+    // range k holds reads [cut[k], cut[k+1]): cut[j] is the first read after the
+    // byte prefix reaches j/t of the total
+    std::vector<size_t> cut((size_t)t + 1, n);
+    cut[0] = 0;
+    int64_t acc = 0;
+    int j = 1;
+    for (size_t i = 0; i < n && j < t; ++i) {
+        acc += (int64_t)read_len[i] + 1 + (int64_t)sizeof(abea_event_t) * (int64_t)et[i].n;
+        while (j < t && acc * t >= total_bytes * j) cut[(size_t)j++] = i + 1;
+    }
+    std::vector<std::thread> th;
+    int started = 1;
+    try {
+        th.reserve((size_t)t - 1);
+        for (; started < t; ++started) th.emplace_back(copy, cut[(size_t)started], cut[(size_t)started + 1]);
+    } catch (...) {
+        // no more threads: the calling thread copies the ranges not started
+    }
+    copy(cut[0], cut[1]);
+    for (int k = started; k < t; ++k) copy(cut[(size_t)k], cut[(size_t)k + 1]);
+    for (auto& x : th) x.join();
+}
+
+// The staging of abea_align_db on its own (no device), for tests: writes the
+// flattened reads and events to seq / ev; returns 0, or -1 on a bad argument.
+extern "C" int32_t abea_internal_stage_db(int32_t n_reads, char* const* read, const int32_t* read_len,
+                                          const abea_event_table_t* et, char* seq, abea_event_t* ev,
+                                          int32_t threads) {
+    if (n_reads < 0 || (n_reads > 0 && (!read || !read_len || !et || !seq || !ev))) return -1;
+    const size_t n = (size_t)n_reads;
+    std::vector<int64_t> read_ptr(n), event_ptr(n);
+    int64_t seq_bytes = 0, events = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (read_len[i] < 0) return -1;
+        read_ptr[i] = seq_bytes;
+        seq_bytes += read_len[i] + 1;
+        event_ptr[i] = events;
+        events += (int64_t)et[i].n;
+    }
+    stage_db(n, read, read_len, et, read_ptr.data(), event_ptr.data(), seq, ev,
+             seq_bytes + (int64_t)sizeof(abea_event_t) * events, threads);
+    return 0;
+}
+
 extern "C" abea_status_t abea_align_db(abea_ctx_t* c, int32_t n_reads, char* const* read, const int32_t* read_len,
                                        const abea_event_table_t* et, const abea_scalings_t* scalings,
                                        const abea_model_t* model, abea_aligned_pair_t* const* pairs,
@@ -1274,11 +1344,8 @@ extern "C" abea_status_t abea_align_db(abea_ctx_t* c, int32_t n_reads, char* con
     char* seq = (char*)c->db_pin;
     abea_event_t* ev = (abea_event_t*)(seq + seq_sz);
     abea_aligned_pair_t* out = (abea_aligned_pair_t*)((char*)ev + ev_sz);
-    for (size_t i = 0; i < n; ++i) {
-        if (read_len[i] > 0) memcpy(seq + read_ptr[i], read[i], (size_t)read_len[i]);
-        seq[read_ptr[i] + read_len[i]] = 0;
-        if (et[i].n > 0) memcpy(ev + event_ptr[i], et[i].event, sizeof(abea_event_t) * et[i].n);
-    }
+    stage_db(n, read, read_len, et, read_ptr.data(), event_ptr.data(), seq, ev,
+             seq_bytes + (int64_t)sizeof(abea_event_t) * events, 0);
     HostInputs in = inputs(n_reads, seq, read_ptr.data(), read_len, ev, event_ptr.data(), n_ev.data(), scalings, model);
     const abea_status_t st = align_batch_impl(c, in, out, n_pairs);
     // per-read statuses (capacity, undefined) leave the other reads' results valid

@@ -1,8 +1,10 @@
 """f5c-facing entries beyond align(): the per-read-array batch call (f5c's db_t,
 `abea_align_db`) and the method-of-moments scalings (f5c's
 estimate_scalings_using_mom, `abea_batch_estimate_scalings`)."""
+import ctypes as C
 import os
 import subprocess
+import time
 
 import numpy as np
 import pytest
@@ -103,3 +105,47 @@ def test_persistent_and_backward_entries(oracle_mod):
     g2 = np.zeros((batch.n_reads, 3))
     abea._check(abea.lib().abea_backward_batch(dev.ctx.h, dev.h, abea._p(g2), None, None, None))
     assert np.array_equal(g["grad_scalings"], g2)
+
+
+def _stage(batch, threads):
+    """abea_align_db's staging of f5c's per-read arrays, on the host alone."""
+    n = batch.n_reads
+    reads = [np.ascontiguousarray(batch.read[batch.read_ptr[i]:batch.read_ptr[i] + batch.read_len[i]])
+             for i in range(n)]
+    evs = [np.ascontiguousarray(batch.events[batch.event_ptr[i]:batch.event_ptr[i] + batch.n_events[i]])
+           for i in range(n)]
+    read_p = (C.c_void_p * max(n, 1))(*[r.ctypes.data if len(r) else None for r in reads])
+    et = (abea._EventTable * max(n, 1))()
+    for i, e in enumerate(evs):
+        et[i].n, et[i].start, et[i].end, et[i].event = len(e), 0, len(e), e.ctypes.data if len(e) else None
+    lens = np.ascontiguousarray(batch.read_len, dtype=np.int32)
+    seq = np.full(int((batch.read_len + 1).sum()), 0x5A, dtype=np.uint8)
+    ev = np.zeros(int(batch.n_events.sum()), dtype=abea.EVENT_DTYPE)
+    f = abea.lib().abea_internal_stage_db
+    f.argtypes = [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+    f.restype = C.c_int32
+    t0 = time.perf_counter()
+    assert f(n, read_p, lens.ctypes.data, C.cast(et, C.c_void_p), seq.ctypes.data, ev.ctypes.data, threads) == 0
+    return seq, ev, time.perf_counter() - t0
+
+
+def test_db_staging_on_host_threads():
+    """The per-read arrays land in the flattened layout (each read NUL terminated,
+    events in order) whatever the number of host threads, with empty reads and
+    reads without events among them."""
+    if not os.path.exists(abea.LIB_PATH):
+        abea.build()
+    from abea_gb300 import synth
+    b = synth.make_batch("f5c_batch", seed=1)
+    seqs = [b.sequence(i) for i in range(b.n_reads)]
+    evs = [b.read_events(i) for i in range(b.n_reads)]
+    seqs[3], evs[5], seqs[7], evs[7] = b"", evs[5][:0], b"", evs[7][:0]
+    b = abea.from_reads(seqs, evs, b.scalings, b.model)
+    for threads in (1, 3, 8, 0):
+        seq, ev, _ = _stage(b, threads)
+        assert np.array_equal(seq, b.read), threads
+        assert np.array_equal(ev.view(np.uint8), np.ascontiguousarray(b.events, dtype=abea.EVENT_DTYPE).view(np.uint8))
+    # more threads than reads
+    small = b.subset([0, 1, 2])
+    seq, ev, _ = _stage(small, 8)
+    assert np.array_equal(seq, small.read)
