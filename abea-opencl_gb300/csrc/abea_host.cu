@@ -1234,52 +1234,61 @@ extern "C" abea_status_t abea_align_batch_persistent(abea_ctx_t* c, int32_t n_re
 
 // f5c's db_t arrays: flatten into pinned staging (GPU/align_cuda.c:432-497's layout),
 // align, unflatten.
-// Copies f5c's per-read arrays into the flattened layout (reads NUL separated
-// from read_ptr[i], events from event_ptr[i]).  Batches of at least
-// kStageMinBytes are split into contiguous ranges of reads of about equal bytes,
-// one per host thread (up to kStageThreads, or `threads` when positive).
-constexpr int kStageThreads = 8;
-constexpr int64_t kStageMinBytes = 8 << 20;
-static void stage_db(size_t n, char* const* read, const int32_t* read_len, const abea_event_table_t* et,
-                     const int64_t* read_ptr, const int64_t* event_ptr, char* seq, abea_event_t* ev,
-                     int64_t total_bytes, int threads) {
-    auto copy = [=](size_t lo, size_t hi) {
-        for (size_t i = lo; i < hi; ++i) {
-            if (read_len[i] > 0) memcpy(seq + read_ptr[i], read[i], (size_t)read_len[i]);
-            seq[read_ptr[i] + read_len[i]] = 0;
-            if (et[i].n > 0) memcpy(ev + event_ptr[i], et[i].event, sizeof(abea_event_t) * et[i].n);
-        }
-    };
+// Runs fn(lo, hi) over contiguous ranges of [0, n) of about equal weight
+// (weight(i) bytes per item, `total` in all), one range per host thread: up to
+// kHostThreads, or `threads` when positive; one call on the calling thread below
+// kHostMinBytes.  A thread that cannot be started leaves its range to the caller.
+constexpr int kHostThreads = 8;
+constexpr int64_t kHostMinBytes = 8 << 20;
+template <class Weight, class Fn>
+static void for_ranges(size_t n, int64_t total, int threads, Weight weight, Fn fn) {
     int t = threads;
     if (t <= 0) {
         const unsigned hw = std::max(std::thread::hardware_concurrency(), 1u);
-        t = total_bytes < kStageMinBytes ? 1 : (int)std::min<unsigned>((unsigned)kStageThreads, hw);
+        t = total < kHostMinBytes ? 1 : (int)std::min<unsigned>((unsigned)kHostThreads, hw);
     }
-    if (t <= 1 || n < 2 || total_bytes <= 0) {
-        copy(0, n);
+    if (t <= 1 || n < 2 || total <= 0) {
+        fn((size_t)0, n);
         return;
     }
-    // range k holds reads [cut[k], cut[k+1]): cut[j] is the first read after the
-    // byte prefix reaches j/t of the total
+    // range k holds items [cut[k], cut[k+1]): cut[j] is the first item after the
+    // weight prefix reaches j/t of the total
     std::vector<size_t> cut((size_t)t + 1, n);
     cut[0] = 0;
     int64_t acc = 0;
     int j = 1;
     for (size_t i = 0; i < n && j < t; ++i) {
-        acc += (int64_t)read_len[i] + 1 + (int64_t)sizeof(abea_event_t) * (int64_t)et[i].n;
-        while (j < t && acc * t >= total_bytes * j) cut[(size_t)j++] = i + 1;
+        acc += weight(i);
+        while (j < t && acc * t >= total * j) cut[(size_t)j++] = i + 1;
     }
     std::vector<std::thread> th;
     int started = 1;
     try {
         th.reserve((size_t)t - 1);
-        for (; started < t; ++started) th.emplace_back(copy, cut[(size_t)started], cut[(size_t)started + 1]);
+        for (; started < t; ++started) th.emplace_back(fn, cut[(size_t)started], cut[(size_t)started + 1]);
     } catch (...) {
-        // no more threads: the calling thread copies the ranges not started
+        // no more threads: the calling thread takes the ranges not started
     }
-    copy(cut[0], cut[1]);
-    for (int k = started; k < t; ++k) copy(cut[(size_t)k], cut[(size_t)k + 1]);
+    fn(cut[0], cut[1]);
+    for (int k = started; k < t; ++k) fn(cut[(size_t)k], cut[(size_t)k + 1]);
     for (auto& x : th) x.join();
+}
+
+// Copies f5c's per-read arrays into the flattened layout: reads NUL separated
+// from read_ptr[i], events from event_ptr[i].
+static void stage_db(size_t n, char* const* read, const int32_t* read_len, const abea_event_table_t* et,
+                     const int64_t* read_ptr, const int64_t* event_ptr, char* seq, abea_event_t* ev,
+                     int64_t total_bytes, int threads) {
+    for_ranges(
+        n, total_bytes, threads,
+        [=](size_t i) { return (int64_t)read_len[i] + 1 + (int64_t)sizeof(abea_event_t) * (int64_t)et[i].n; },
+        [=](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; ++i) {
+                if (read_len[i] > 0) memcpy(seq + read_ptr[i], read[i], (size_t)read_len[i]);
+                seq[read_ptr[i] + read_len[i]] = 0;
+                if (et[i].n > 0) memcpy(ev + event_ptr[i], et[i].event, sizeof(abea_event_t) * et[i].n);
+            }
+        });
 }
 
 // The staging of abea_align_db on its own (no device), for tests: writes the
@@ -1350,8 +1359,16 @@ extern "C" abea_status_t abea_align_db(abea_ctx_t* c, int32_t n_reads, char* con
     const abea_status_t st = align_batch_impl(c, in, out, n_pairs);
     // per-read statuses (capacity, undefined) leave the other reads' results valid
     if (st != ABEA_OK && st != ABEA_ERR_CAPACITY && st != ABEA_ERR_UNDEFINED) return st;
-    for (size_t i = 0; i < n; ++i)
-        if (n_pairs[i] > 0) memcpy(pairs[i], out + 2 * event_ptr[i], sizeof(abea_aligned_pair_t) * (size_t)n_pairs[i]);
+    int64_t out_bytes = 0;
+    for (size_t i = 0; i < n; ++i) out_bytes += (int64_t)sizeof(abea_aligned_pair_t) * std::max(n_pairs[i], 0);
+    const int64_t* ep = event_ptr.data();
+    for_ranges(
+        n, out_bytes, 0, [=](size_t i) { return (int64_t)sizeof(abea_aligned_pair_t) * std::max(n_pairs[i], 0); },
+        [=](size_t lo, size_t hi) {
+            for (size_t i = lo; i < hi; ++i)
+                if (n_pairs[i] > 0)
+                    memcpy(pairs[i], out + 2 * ep[i], sizeof(abea_aligned_pair_t) * (size_t)n_pairs[i]);
+        });
     return st;
 }
 
