@@ -206,8 +206,10 @@ abea_status_t abea_align_batch_persistent(abea_ctx_t *ctx, int32_t n_reads, cons
 /* f5c's per-read arrays (db_t's read[i], read_len[i], et[i], scalings[i],
  * event_align_pairs[i], n_event_align_pairs[i]; GPU/f5c.h) aligned as one batch:
  * the flattening of GPU/align_cuda.c:432-497 done inside the library, through
- * pinned staging kept by the context.  event_align_pairs[i] must hold
- * 2*et[i].n pairs; n_event_align_pairs[i] as in abea_align_batch. */
+ * pinned staging kept by the context (copied on up to eight host threads for
+ * batches of 8 MB or more, as are the results back to event_align_pairs[i]).
+ * event_align_pairs[i] must hold 2*et[i].n pairs; n_event_align_pairs[i] as in
+ * abea_align_batch. */
 abea_status_t abea_align_db(abea_ctx_t *ctx, int32_t n_reads, char *const *read, const int32_t *read_len,
                             const abea_event_table_t *et, const abea_scalings_t *scalings,
                             const abea_model_t *model, abea_aligned_pair_t *const *event_align_pairs,
