@@ -51,11 +51,24 @@ def test_oracle_mom_is_close_to_the_generating_scalings(oracle_mod):
 @pytest.mark.parametrize("mode", [abea.MODE_PLAIN, abea.MODE_BATCHED])
 def test_align_db_equals_align_batch(mode, ref_synthetic):
     from abea_gb300 import synth
-    for batch in (synth.make_batch("small", seed=6), ref_synthetic[0]):
+    # 64 reads of 9-13 kb that pass QC: over 8 MB both ways, so the staging and the
+    # copy of the results back run on several host threads
+    rng = np.random.default_rng(21)
+    model = synth.make_model(rng)
+    seqs, evs = [], []
+    for L in rng.integers(9000, 13000, 64):
+        s, e = synth.make_read(rng, model, int(L), 1.0, 2.0, 1.2, skip_p=0.005)
+        seqs.append(s.tobytes())
+        evs.append(e)
+    sc = np.array([(1.0, 2.0, 1.2, np.log(1.2))] * len(seqs), dtype=abea.types.SCALINGS_DTYPE)
+    big = abea.from_reads(seqs, evs, sc, model)
+    for batch in (synth.make_batch("small", seed=6), ref_synthetic[0], big):
         ctx = abea.Context(0, mode)
         pairs, counts = ctx.align_batch(batch)
         per_read, c2 = ctx.align_db(batch)
         assert np.array_equal(counts, c2)
+        if batch is big:
+            assert np.maximum(counts, 0).sum() * 8 > 8 << 20
         for x, y in zip(abea.split_pairs(batch, pairs, counts), per_read):
             assert np.array_equal(x, y)
 
