@@ -60,3 +60,22 @@ def test_status_strings_without_device(libpath):
     L = abea.lib()
     assert L.abea_status_string(-2).decode().startswith("alignment longer")
     assert L.abea_version().decode().startswith("abea-gb300")
+
+
+def test_argument_checks_without_device(libpath):
+    """Entries that are handed null handles fail with ABEA_ERR_INVALID_ARG before
+    touching a device (no GPU is needed to reach these checks)."""
+    import ctypes as C
+    L = abea.lib()
+    vp = C.c_void_p
+    L.abea_batch_postalign.argtypes = [vp] * 6
+    assert L.abea_batch_postalign(None, None, None, None, None, None) == -1
+    L.abea_batch_estimate_scalings.argtypes = [vp, vp, vp, C.c_int32]
+    assert L.abea_batch_estimate_scalings(None, None, None, 0) == -1
+    L.abea_align_db.argtypes = [vp, C.c_int32] + [vp] * 7
+    assert L.abea_align_db(None, 1, None, None, None, None, None, None, None) == -1
+    f = L.abea_internal_stage_db
+    f.argtypes = [C.c_int32] + [vp] * 5 + [C.c_int32]
+    f.restype = C.c_int32
+    assert f(-1, None, None, None, None, None, 0) == -1
+    assert f(0, None, None, None, None, None, 0) == 0
