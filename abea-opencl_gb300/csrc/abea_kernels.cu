@@ -531,79 +531,54 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 }
 
 // ---------------------------------------------------------------- wide shape
-// Sixteen warps per read in four groups of 128 threads; thread t of a group
-// works on slot t.  One barrier per band: B_b, once band b's scores are in shared
-// memory.  Between B_{b-1} and B_b:
-//   B  (warps 0-3)    band b only: the up candidate from this slot's own band
-//                     b-1 score, the end and left-neighbour cells of band b-1,
-//                     the placement, the exact skip candidate, the comparison
-//                     and the stores.  Everything else runs in the other groups,
-//                     so that B's loop body is one short block.
-//   D  (warps 4-7)    places band b too and prepares band b+1: the exact
-//                     diagonal candidate (from band b-1's left neighbour), which
-//                     cells lie inside the read and the band for either move,
-//                     and the trim cell's value.
-//   E0 (warps 8-11)   even b: band b+2's emissions and their exact splits, with
-//   E1 (warps 12-15)  odd b the k-mer assignment of band b-1 (a slot keeps its
-//                     k-mer for as long as it can be inside the band); the other
-//                     half does band b-1's bookkeeping (last k-mer column, band
-//                     origin, trace stores of four bands per 32-bit word).  E0
-//                     also runs the prefetch rings.
+// Twelve warps per read (the block's other warps wait at its next barrier):
+//   B (warps 0-3)   the band-to-band chain, one k-mer slot per thread.  Per band:
+//                   the end cells and the left neighbour of band b-1 from shared
+//                   memory, the placement, the in-band test, the exact up and
+//                   diagonal candidates (both from registers), the exact skip
+//                   candidate, the comparison, and the
+//                   bookkeeping (backpointers packed four bands to a word and
+//                   stored once per tile, band origins packed one per lane,
+//                   last k-mer column).  One 128-thread named barrier per band.
+//   E (warps 4-11)  the emissions and their exact splits, kWideChunk bands at a
+//                   time for the thread's slot (a slot keeps its k-mer while its
+//                   event advances by one per band: one load of its pore-model
+//                   parameters per chunk), up to kWideRing chunks ahead of B, into a
+//                   ring in shared memory; warps 4-7 take the even chunks, warps
+//                   8-11 the odd ones.
+// A band's cells lie on one anti-diagonal, so the placement of any band p with
+// bn - p <= 28 gives a window [k0(p), k0(p) + 128) that holds band bn's k-mers
+// (each band moves k0 by at most one): E computes a chunk from the placement B
+// published when it released the ring slot, kWideChunk * kWideRing + 1 = 17
+// bands before the chunk's last band.  B and E hand the ring slots over with
+// named barriers, FULL[s] (E arrives, B waits) and EMPTY[s] (B arrives, E waits);
+// every use of a barrier completes before its next, so arrivals never pile up.
+constexpr int kWideThreads = 512;   // block size of the batched kernel
+constexpr int kWideChunk = 4;       // bands per emission chunk
+constexpr int kWideRing = 4;        // chunks in the ring (kWideChunk * kWideRing + 1 <= 28)
+constexpr int kBarChain = 1;        // B's per-band barrier
+constexpr int kBarFull = 2;         // FULL[s] = kBarFull + s
+constexpr int kBarEmpty = kBarFull + kWideRing;  // EMPTY[s] = kBarEmpty + s
+static_assert(kWideChunk * kWideRing + 1 <= 28, "E's k-mer window must hold the chunk's bands");
+static_assert(kWideRing % 2 == 0, "each ring slot, and its two barriers, belongs to one of the two E groups");
+static_assert(kBarEmpty + kWideRing <= 16, "named barriers 0-15");
+
 struct alignas(16) WideSmem {
-    Rings rg;
-    float sc[2][kSlots];                       // band scores, buffer b & 1
-    // emission of band b, buffer b & 3: {stay split p, w; |em| + |stay_h| (NaN when the
-    // division is not proven); em} and {step split p, w} (one vector access each)
-    float4 emu[4][kSlots];
-    float2 emd[4][kSlots];
-    float dc[2][kSlots];                       // exact diagonal candidate of band b
-    int32_t flags[2][kSlots];                  // band b: 1 inside if down, 2 inside if right, 4 d proven
-    float trim[2];                             // band b's trim cell value (-inf: outside the read)
-    uint32_t fr[8][kSlots];                    // backpointer of band b at [b & 7]
-    int32_t k0h[8];                            // lower-left k-mer of band b at [b & 7]
+    // band kWideChunk*j + 2 + q of chunk j in slot j % kWideRing, entry [q]:
+    // {p_step, p_stay, w_step, w_stay} and {|em| + |step_h|, |em| + |stay_h|} (NaN
+    // when the emission's division was not proven)
+    float4 ems[kWideRing][kWideChunk][kSlots];
+    float2 emm[kWideRing][kWideChunk][kSlots];
+    float sc[2][kSlots];                  // band scores, buffer b & 1
+    float trim[kWideRing][kWideChunk];    // the trim cell's value of each band (-inf: past the read's events)
+    int32_t k0h[64];                      // placement of band b at [b & 63], for E
 };
 
-constexpr int kWideThreads = 512;
-
-// Named barrier 1 over the block: the groups reach it from different code
-// paths, once per band each.
-__device__ __forceinline__ void wide_barrier() { asm volatile("bar.sync 1, 512;\n" ::: "memory"); }
-
-// E: emission of slot t for the band whose event for this slot is e, into buffer
-// buf (band & 3: written two bands ahead while B reads the current band's).
-__device__ __forceinline__ void wide_emission(WideSmem& ws, const CellConsts& cc, int t, int buf, int e) {
-    bool ok;
-    const float em = emission_fast(ws.rg.ev[e & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t], ws.rg.rsd[t],
-                                   ws.rg.k1[t], ok);
-    const EmSplit s1 = em_split(em, cc.step_h, cc.step_l);
-    const EmSplit s2 = em_split(em, cc.stay_h, cc.stay_l);
-    ws.emu[buf][t] = make_float4(s2.p, s2.w, ok ? __fadd_rn(fabsf(em), fabsf(cc.stay_h)) : __int_as_float(0x7fc00000),
-                                 em);
-    ws.emd[buf][t] = make_float2(s1.p, s1.w);
+__device__ __forceinline__ void named_bar_sync(int id, int n) {
+    asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(n) : "memory");
 }
-
-// D: band bn's diagonal candidate from `diag`, its inside flags and trim value,
-// with the band before it placed at k0.
-__device__ __forceinline__ void wide_diag(WideSmem& ws, const CellConsts& cc, const GlobalConsts& g, int t, int bn,
-                                          float diag, int k0, int n_events, int n_kmers) {
-    const int buf = bn & 1, ebuf = bn & 3;
-    const float em = ws.emu[ebuf][t].w;
-    const float2 sd = ws.emd[ebuf][t];
-    const EmSplit s1{sd.x, sd.y};
-    bool okd;
-    const float d = exact_from_split(diag, s1, __fadd_rn(fabsf(em), fabsf(cc.step_h)), fabsf(em) < INFINITY, okd);
-    const int o = (t - k0) & 127;
-    const int kk = k0 + o;
-    const int e = bn - 2 - kk;
-    const bool inb = (kk >= 0) && (kk < n_kmers) && (e >= 0) && (e < n_events);
-    const int f = ((inb && o < kBand) ? 1 : 0) | ((inb && o >= 1 && o <= kBand) ? 2 : 0) | (okd ? 4 : 0);
-    ws.dc[buf][t] = d;
-    ws.flags[buf][t] = f;
-    if (k0 <= 0 && t == 0) {
-        // trim cell of band bn (k = -1): event bn - 1, (float)(lp_trim * (e + 1)) (GPU/align_cuda.cl:431-443)
-        const int e_t = bn - 1;
-        ws.trim[buf] = (e_t < n_events) ? __double2float_rn(__dmul_rn(g.lp_trim, (double)(e_t + 1))) : -INFINITY;
-    }
+__device__ __forceinline__ void named_bar_arrive(int id, int n) {
+    asm volatile("bar.arrive %0, %1;\n" ::"r"(id), "r"(n) : "memory");
 }
 
 __device__ __forceinline__ bool band_moves_right(float ll, float ur, int b) {
@@ -611,169 +586,207 @@ __device__ __forceinline__ bool band_moves_right(float ll, float ur, int b) {
     return (ll == -INFINITY && ur == -INFINITY) ? (bool)(b & 1) : (ll < ur);
 }
 
-// Called by all 512 threads of a block.
+// E: chunk j's emissions for slot t, from the placement kp of an earlier band.
+__device__ __forceinline__ void wide_chunk(WideSmem& ws, const CoreArgs& a, const ReadDesc& r, const CellConsts& cc,
+                                           int t, int j, int kp) {
+    const int s = j & (kWideRing - 1), bb = 2 + kWideChunk * j;
+    const int kk = kp + ((t - kp) & (kSlots - 1));  // slot t's k-mer in the window
+    const bool kin = kk >= 0 && kk < r.n_kmers;
+    const int64_t ko = r.km_off + (kin ? kk : 0);
+    const float gm = a.km_gm[ko], sd = a.km_sd[ko], rsd = a.km_rsd[ko], k1 = a.km_k1[ko];
+    const float* ev = a.ev_mean + r.ev_off;
+    const int e_first = bb - 2 - kk;
+    float x[kWideChunk];
+#pragma unroll
+    for (int q = 0; q < kWideChunk; ++q) {
+        // cells outside the read get a finite stand-in; B's in-band test keeps them out
+        const int e = e_first + q;
+        x[q] = (kin && e >= 0 && e < r.n_events) ? ev[e] : gm;
+    }
+#pragma unroll
+    for (int q = 0; q < kWideChunk; ++q) {
+        bool ok;
+        const float em = emission_fast(x[q], gm, sd, rsd, k1, ok);
+        const EmSplit s1 = em_split(em, cc.step_h, cc.step_l);
+        const EmSplit s2 = em_split(em, cc.stay_h, cc.stay_l);
+        const float nan = __int_as_float(0x7fc00000);
+        ws.ems[s][q][t] = make_float4(s1.p, s2.p, s1.w, s2.w);
+        ws.emm[s][q][t] = ok ? make_float2(__fadd_rn(fabsf(em), fabsf(cc.step_h)), __fadd_rn(fabsf(em), fabsf(cc.stay_h)))
+                             : make_float2(nan, nan);
+    }
+    if (t < kWideChunk) {
+        // the trim cell (k = -1) of band bb + t: event bb + t - 1, (float)(lp_trim * (e + 1))
+        // (GPU/align_cuda.cl:431-443); B uses it while the band reaches below k-mer 0
+        const int e_t = bb + t - 1;
+        ws.trim[s][t] = e_t < r.n_events ? __double2float_rn(__dmul_rn(a.g.lp_trim, (double)(e_t + 1))) : -INFINITY;
+    }
+}
+
+// The reference's arithmetic for one cell whose exactness proof failed, as a
+// call: its division routine and FP64 code stay out of the band loop's body.
+struct SlowCell {
+    float best;
+    uint32_t from;
+};
+__device__ __noinline__ SlowCell slow_cell_call(float diag, float up, float left, float x, float gm, float sd, float k1,
+                                                double lp_step, double lp_stay, double lp_skip) {
+    CellConsts c{};
+    c.lp_step = lp_step;
+    c.lp_stay = lp_stay;
+    c.lp_skip = lp_skip;
+    SlowCell o;
+    o.best = cell_slow(diag, up, left, x, gm, sd, k1, c, o.from);
+    return o;
+}
+
+// Called by all kWideThreads threads of a block; warps 12 and up return at once.
 template <bool kScores>
 __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, int tid) {
+    const int warp = tid >> 5;
+    if (warp >= 12) return;
     const CellConsts cc = make_consts(r, a.g);
     const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
-    const int group = tid >> 7;  // 0 = B, 1 = D, 2 = E0, 3 = E1
+    const int n_chunks = (n_bands - 2 + kWideChunk - 1) / kWideChunk;
     const int t = tid & (kSlots - 1);
-    const int ring_t = group == 2 ? t : 1000;  // E0 runs the rings
+    constexpr int kPair = 2 * kSlots;  // B and E threads on FULL / EMPTY
 
-    int k0 = -1 - kBand / 2, e0 = kBand / 2;  // band 1 (band 0 is (49,-51), band 1 moved down)
-    RingState rs;
-    rings_init(ws.rg, rs, a, r, ring_t, k0, e0);
-    if (group == 0) {
-        ws.sc[1][t] = (t == 127) ? a.g.trim_f : -INFINITY;
-        ws.fr[0][t] = 0u;
-        ws.fr[1][t] = (t == 127) ? ABEA_FROM_U : 0u;
-    } else if (group == 1 && t == 0) {
-        ws.k0h[0] = k0;
-        ws.k0h[1] = k0;
-        a.band_k0[r.band_off] = k0;
-    }
-    wide_barrier();
-    if (group >= 2) {
-        // bands 2 (E0) and 3 (E1) under band 1's k-mer assignment: event = band - 2 - k-mer
-        const int kk = k0 + ((t - k0) & 127);
-        const int bn = group == 2 ? 2 : 3;
-        wide_emission(ws, cc, t, bn & 3, bn - 2 - kk);
-    }
-    wide_barrier();
-    if (group == 0) {
-        // ------------------------------------------------ B: the critical path
-        float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
-        float s_prev = (t == 127) ? a.g.trim_f : -INFINITY;  // band 1
-        float lp = (t == 0) ? 0.0f : -INFINITY;              // band 0 shifted by one slot
-        if (kScores) {
-            scores[t] = (t == 127) ? 0.0f : -INFINITY;
-            scores[kSlots + t] = s_prev;
-        }
-        unsigned long long slow = 0;
-        // Band state kept across the exit to the slow path.  A band in which a
-        // proof failed in any lane of the warp leaves the inner loop
-        // (warp-uniform) and is finished below with the reference's FP64
-        // arithmetic: the inner loop holds no division routine and no FP64 code.
-        int b = 2, cb = 0;
-        float best = 0.0f, left = 0.0f;
-        uint32_t from = 0u;
-        bool valid = false, bad = false;
-        auto finish = [&]() {
-            best = valid ? best : -INFINITY;
-            from = valid ? from : 0u;
-            // trim cell (k = -1, slot 127) while the band still reaches below k-mer 0
-            const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
-            const float tv = ws.trim[cb];
-            best = here ? tv : best;
-            from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
-            ws.sc[cb][t] = best;
-            ws.fr[b & 7][t] = from;
-            if (kScores && in_bounds(b, n_bands, a.counters)) scores[(int64_t)b * kSlots + t] = best;
-            lp = left;
-            s_prev = best;
-        };
-        while (true) {
-            bool to_slow = false;
-            for (; b < n_bands; ++b) {
-                wide_barrier();  // B_{b-1}
-                const int pb = (b - 1) & 1;
-                cb = b & 1;
-                const float ll = ws.sc[pb][k0 & 127];
-                const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
-                left = ws.sc[pb][(t + 127) & 127];
-                const float d = ws.dc[cb][t];
-                const int f = ws.flags[cb][t];
-                const float4 eu = ws.emu[b & 3][t];
-                const EmSplit su{eu.x, eu.y};
-                const float mu = eu.z;
-                // up candidate from this slot's own band b-1 score
-                bool oku;
-                const float u = exact_from_split(s_prev, su, mu, mu < INFINITY, oku);
-                const bool right = band_moves_right(ll, ur, b);
-                k0 += right ? 1 : 0;
-                e0 += right ? 0 : 1;
-                valid = (f & (right ? 2 : 1)) != 0;
-                // d vs u (U wins ties), then the skip candidate (L wins ties)
-                uint32_t from_du;
-                const float best_du = pick_du(d, u, from_du);
-                bool okl;
-                const float l = exact_skip(left, cc.skip_h, cc.skip_l, okl);
-                best = pick_l(best_du, from_du, l, from);
-                bad = valid && !(oku && okl && (f & 4));
-                if (__any_sync(kFull, bad)) {
-                    to_slow = true;
-                    break;
-                }
-                finish();
+    if (warp >= 4) {
+        // ------------------------------------------------ E: the emission chunks,
+        // E0 (warps 4-7) the even ones, E1 (warps 8-11) the odd ones: each group has
+        // two chunks of B's time for the loads and arithmetic of one
+        for (int j = (warp >> 2) - 1; j < n_chunks; j += 2) {
+            const int s = j & (kWideRing - 1);
+            int kp = -1 - kBand / 2;  // band 1's placement, for the first kWideRing chunks
+            if (j >= kWideRing) {
+                named_bar_sync(kBarEmpty + s, kPair);  // B released chunk j - kWideRing
+                kp = ws.k0h[(kWideChunk * (j - kWideRing) + kWideChunk) & 63];  // band bb(j - R) + C - 2
             }
-            if (!to_slow) break;
-            if (bad) {  // a proof failed: the reference's FP64 arithmetic
-                const int ep = e0 - ((t - k0) & 127);
-                best = cell_slow(lp, s_prev, left, ws.rg.ev[ep & (kEvRing - 1)], ws.rg.gm[t], ws.rg.sd[t],
-                                 ws.rg.k1[t], cc, from);
-                ++slow;
-            }
-            finish();
-            ++b;
+            wide_chunk(ws, a, r, cc, t, j, kp);
+            named_bar_arrive(kBarFull + s, kPair);
         }
-        wide_barrier();  // B_{n_bands-1}
-        if (slow) atomicAdd(&a.counters[0], slow);
-    } else if (group == 1) {
-        // ------------------------------------------------ D
-        wide_diag(ws, cc, a.g, t, 2, (t == 0) ? 0.0f : -INFINITY, k0, n_events, n_kmers);
-        for (int b = 2; b < n_bands; ++b) {
-            wide_barrier();  // B_{b-1}
+        return;
+    }
+
+    // ------------------------------------------------ B: the chain
+    // One iteration per chunk, its kWideChunk bands unrolled: the chunk's barriers
+    // and the backpointer tile stores fall on fixed bands.  Band b-1's bookkeeping
+    // (backpointers, band origin, last k-mer column, scores) runs just after band
+    // b's barrier, beside the loads, so that nothing but the chain stands between
+    // a band's comparison and the next barrier.
+    const int lane = tid & 31;
+    uint8_t* trace = a.trace + r.trace_off * kSlots;
+    int32_t* bk0 = a.band_k0 + r.band_off;
+    float* lastc = a.last_col + r.ev_off;
+    float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
+    const int sl_last = (n_kmers - 1) & (kSlots - 1);
+
+    int k0 = -1 - kBand / 2, e0 = kBand / 2;         // band 1 (band 0 is (49,-51), band 1 moved down)
+    float s1 = (t == 127) ? a.g.trim_f : -INFINITY;  // band b-1's score of this slot
+    float lp = (t == 0) ? 0.0f : -INFINITY;          // band b-2's score of slot t-1: band b's diagonal
+    ws.sc[1][t] = s1;
+    if (kScores) {
+        scores[t] = (t == 127) ? 0.0f : -INFINITY;
+        scores[kSlots + t] = s1;
+    }
+    int my_k0 = k0;                                      // band origins: band b in lane b & 31
+    uint32_t tw = 0u;                                    // backpointers of bands 4m..4m+3, byte b & 3
+    uint32_t from_p = (t == 127) ? ABEA_FROM_U : 0u;     // band b-1's backpointer (band 1: the trim cell)
+    int k0p = k0, e0p = e0, lop = 0, hip = 0;            // band b-1's placement and computed offsets
+    unsigned long long slow = 0;
+    // band bk's bookkeeping; q1 = bk & 3 when known at compile time, else -1
+    auto book = [&](int bk, int q1) {
+        const int qq = q1 >= 0 ? q1 : (bk & 3);
+        tw |= from_p << (8 * qq);
+        my_k0 = ((bk & 31) == lane) ? k0p : my_k0;
+        const int ol = n_kmers - 1 - k0p;  // last k-mer column (GPU/align_cuda.cl:722-746)
+        if (t == sl_last && ol >= lop && ol < hip && in_bounds(e0p - ol, n_events, a.counters))
+            lastc[e0p - ol] = s1;
+        if (kScores && in_bounds(bk, n_bands, a.counters)) scores[(int64_t)bk * kSlots + t] = s1;
+    };
+    auto store_tile = [&](int bk) {
+        if (in_bounds(bk >> 2, (n_bands + 3) / 4, a.counters))
+            reinterpret_cast<uint32_t*>(trace + (int64_t)(bk >> 2) * 512)[t] = tw;
+        tw = 0u;
+    };
+    auto store_origins = [&](int bk) {  // bands (bk & ~31) .. bk
+        if (warp == 0 && lane <= (bk & 31) && in_bounds((bk & ~31) + lane, n_bands, a.counters))
+            bk0[(bk & ~31) + lane] = my_k0;
+    };
+    for (int j = 0; j < n_chunks; ++j) {
+        const int s = j & (kWideRing - 1), bb = 2 + kWideChunk * j;
+#pragma unroll
+        for (int q = 0; q < kWideChunk; ++q) {
+            const int b = bb + q;
+            if (b >= n_bands) break;
+            named_bar_sync(kBarChain, kSlots);                   // band b-1's scores are in shared memory
+            if (q == 0) named_bar_sync(kBarFull + s, kPair);     // chunk j's emissions are in the ring
             const int pb = (b - 1) & 1;
             const float ll = ws.sc[pb][k0 & 127];
             const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
+            const float left = ws.sc[pb][(t + 127) & 127];
+            const float4 ep = ws.ems[s][q][t];
+            const float2 mm = ws.emm[s][q][t];
+            const float tv = ws.trim[s][q];
+            // band b-1's bookkeeping (bands 2 + 4j + q - 1: b-1 & 3 == (q + 1) & 3)
+            book(b - 1, (q + 1) & 3);
+            if (q == 2) {  // band b-1 closes a tile of four bands
+                store_tile(b - 1);
+                if (((b - 1) & 31) == 31) store_origins(b - 1);
+            }
+            if (q == 3 && t == 0) ws.k0h[(b - 1) & 63] = k0p;  // the placement E reads for chunk j + kWideRing
+            // the exact diagonal and up candidates of band b
+            bool okd, oku;
+            const float d = exact_from_split(lp, EmSplit{ep.x, ep.z}, mm.x, mm.x < INFINITY, okd);
+            const float u = exact_from_split(s1, EmSplit{ep.y, ep.w}, mm.y, mm.y < INFINITY, oku);
             const bool right = band_moves_right(ll, ur, b);
             k0 += right ? 1 : 0;
-            if (t == 0) ws.k0h[b & 7] = k0;
-            if (b + 1 < n_bands)
-                wide_diag(ws, cc, a.g, t, b + 1, ws.sc[pb][(t + 127) & 127], k0, n_events, n_kmers);
-        }
-        wide_barrier();  // B_{n_bands-1}
-    } else {
-        // ------------------------------------------------ E0 / E1
-        const int half = group - 2;
-        uint8_t* trace = a.trace + r.trace_off * kSlots;
-        int32_t* bk0 = a.band_k0 + r.band_off;
-        float* lastc = a.last_col + r.ev_off;
-        const int sl_last = (n_kmers - 1) & 127;
-        for (int b = 2; b <= n_bands; ++b) {
-            wide_barrier();  // B_{b-1}
-            const int bp = b - 1;
-            const int kp = ws.k0h[bp & 7];  // band b-1's placement
-            if ((b & 1) == half) {
-                // band b+2's emissions under band b-1's k-mer assignment
-                if (b + 2 < n_bands) wide_emission(ws, cc, t, (b + 2) & 3, b - (kp + ((t - kp) & 127)));
-                if (half == 0 && (b & 3) == 2) rings_step(ws.rg, rs, a, r, ring_t, kp, bp - 2 - kp, 9);
-            } else {
-                // band b-1's bookkeeping
-                const int ep0 = bp - 2 - kp;
-                const int ol = n_kmers - 1 - kp;
-                if (ol < kBand && t == sl_last && bp >= 2) {  // last k-mer column (GPU/align_cuda.cl:722-746)
-                    int lo, hi;
-                    band_range(kp, ep0, n_events, n_kmers, lo, hi);
-                    if (ol >= lo && ol < hi && in_bounds(ep0 - ol, n_events, a.counters))
-                        lastc[ep0 - ol] = ws.sc[bp & 1][t];
-                }
-                if (t == 0 && in_bounds(bp, n_bands, a.counters)) bk0[bp] = kp;
-                if ((bp & 3) == 3 || bp == n_bands - 1) {
-                    // four bands of backpointers, byte j = band 4q + j (bands past the read: 0)
-                    const int q0 = bp & ~3, nj = bp - q0;
-                    uint32_t word = 0u;
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (j <= nj) word |= (ws.fr[(q0 + j) & 7][t] & 0xffu) << (8 * j);
-                    if (in_bounds(bp >> 2, (n_bands + 3) / 4, a.counters))
-                        reinterpret_cast<uint32_t*>(trace + (int64_t)(bp >> 2) * 512)[t] = word;
+            e0 += right ? 0 : 1;
+            int lo, hi;
+            band_range(k0, e0, n_events, n_kmers, lo, hi);
+            const int o = (t - k0) & 127;
+            const bool valid = o >= lo && o < hi;
+            // d vs u (U wins ties), then the skip candidate (L wins ties)
+            uint32_t from_du, from;
+            const float best_du = pick_du(d, u, from_du);
+            bool okl;
+            const float l = exact_skip(left, cc.skip_h, cc.skip_l, okl);
+            float best = pick_l(best_du, from_du, l, from);
+            const bool bad = valid && !(okd && oku && okl);
+            if (__any_sync(kFull, bad)) {  // warp-uniform and rare
+                if (bad) {  // a proof failed: the reference's FP64 arithmetic
+                    const int64_t ko = r.km_off + (k0 + o);
+                    const SlowCell c = slow_cell_call(lp, s1, left, a.ev_mean[r.ev_off + (e0 - o)], a.km_gm[ko],
+                                                      a.km_sd[ko], a.km_k1[ko], cc.lp_step, cc.lp_stay, cc.lp_skip);
+                    best = c.best;
+                    from = c.from;
+                    ++slow;
                 }
             }
+            best = valid ? best : -INFINITY;
+            from = valid ? from : 0u;
+            // the trim cell (k = -1, slot 127) while the band reaches below k-mer 0
+            const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
+            best = here ? tv : best;
+            from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
+            ws.sc[b & 1][t] = best;
+            if (q == kWideChunk - 1 && j + kWideRing < n_chunks)
+                named_bar_arrive(kBarEmpty + s, kPair);  // chunk j read: E may refill its slot
+            lp = left;
+            s1 = best;
+            from_p = from;
+            k0p = k0;
+            e0p = e0;
+            lop = lo;
+            hip = hi;
         }
     }
-    cp_async_wait_all();
-    wide_barrier();
+    if (n_bands > 2) {  // the last band's bookkeeping and the stores it closes
+        const int bl = n_bands - 1;
+        book(bl, -1);
+        store_tile(bl);
+        store_origins(bl);
+    }
+    if (slow) atomicAdd(&a.counters[0], slow);
 }
 
 // ---------------------------------------------------------------- wide shape on a cluster pair
@@ -1893,8 +1906,8 @@ static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSme
                   sizeof(Rings) % 16 == 0 && sizeof(PostSmem) % 16 == 0,
               "cp.async destinations must be 16-byte aligned");
 static_assert(sizeof(BatchedSmem) <= 227 * 1024, "batched kernel shared memory exceeds the per-block limit");
-static_assert(offsetof(WideSmem, emu) % 16 == 0 && offsetof(WideSmem, emd) % 8 == 0,
-              "vector accesses to the emission buffers must be aligned");
+static_assert(offsetof(WideSmem, ems) % 16 == 0 && offsetof(WideSmem, emm) % 8 == 0,
+              "vector accesses to the emission ring must be aligned");
 static_assert(sizeof(WideSmem) >= kPostRingDeep * kPostChunkBands * kSlots && alignof(WideSmem) >= 16,
               "the wide read's traceback ring lives in the wide fill's shared memory");
 static_assert(sizeof(WidePostSmem) <= sizeof(WideSmem), "the wide read's traceback state fits the fill's memory");
@@ -2115,8 +2128,65 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 __global__ void noalloc_write_desc(ReadDesc* dst, ReadDesc d) { *dst = d; }
 
+// The array's device address differs per CUDA context: one per device for the
+// runtime's primary contexts, a new one after cudaDeviceReset, and one in each
+// context a caller creates itself.  The addresses are kept per context, keyed by
+// the context's process-unique id (cuCtxGetId; a context's handle may be reused
+// after a reset, its id is not).  The two driver calls are found through the
+// runtime (cudaGetDriverEntryPointByVersion), so the library needs no link
+// against the driver library.
 static std::mutex g_noalloc_mutex;
-static void* g_noalloc_ptr[256];  // device address of g_noalloc_scratch, per device
+struct NoAllocSlot {
+    unsigned long long ctx_id;
+    void* ptr;
+};
+static NoAllocSlot g_noalloc_slots[64];  // most recently looked up first
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+
+// Id of the current context, 0 when none is current or the driver calls are missing.
+static unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = (CtxGetCurrentFn)f1;
+            get_id = (CtxGetIdFn)f2;
+        }
+        looked_up = true;
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_scratch in the current context: looked up with
+// cudaGetSymbolAddress the first time a context asks, then kept.  nullptr on failure.
+static void* noalloc_scratch_address(cudaError_t* err) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    unsigned long long id = current_ctx_id();
+    if (id != 0) {
+        for (int i = 0; i < 64 && g_noalloc_slots[i].ptr; ++i)
+            if (g_noalloc_slots[i].ctx_id == id) return g_noalloc_slots[i].ptr;
+    }
+    void* p = nullptr;
+    *err = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // makes the device's primary context current if none is
+    if (*err != cudaSuccess || !p) return nullptr;
+    if (id == 0) id = current_ctx_id();
+    if (id != 0) {  // keep it, most recent first (the oldest of a full table is dropped)
+        for (int i = 63; i > 0; --i) g_noalloc_slots[i] = g_noalloc_slots[i - 1];
+        g_noalloc_slots[0] = NoAllocSlot{id, p};
+    }
+    return p;
+}
 
 static size_t noalloc_align(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -2149,32 +2219,25 @@ extern "C" abea_status_t abea_align_noalloc(abea_aligned_pair_t* pairs, int32_t*
         char msg[256];
         snprintf(msg, sizeof(msg),
                  "abea_align_noalloc: the read needs %zu bytes of scratch but the fixed scratch holds %zu "
-                 "bytes (reads of up to about 250,000 bands, n_events + n_kmers + 2)",
+                 "bytes (reads of up to about 230,000 bands, n_events + n_kmers + 2)",
                  need, kNoAllocScratchBytes);
         abea_internal_set_error(msg);
         return ABEA_ERR_INVALID_ARG;
     }
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
         abea_internal_set_error("abea_align_noalloc: no current CUDA device");
         return ABEA_ERR_NO_DEVICE;
     }
-    unsigned char* base = nullptr;
-    {
-        // once per device, with that device current: the array's device address
-        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) {
-                char msg[256];
-                snprintf(msg, sizeof(msg), "abea_align_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-                abea_internal_set_error(msg);
-                return ABEA_ERR_CUDA;
-            }
-            g_noalloc_ptr[dev] = p;
-        }
-        base = (unsigned char*)g_noalloc_ptr[dev];
+    // the first call in each context (per device, and again after a device
+    // reset) looks up the array's address; later calls reuse it
+    cudaError_t serr = cudaSuccess;
+    unsigned char* base = (unsigned char*)noalloc_scratch_address(&serr);
+    if (!base) {
+        char msg[256];
+        snprintf(msg, sizeof(msg), "abea_align_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(serr));
+        abea_internal_set_error(msg);
+        return ABEA_ERR_CUDA;
     }
     cudaStream_t st = (cudaStream_t)stream;
     const int32_t nk = sequence_len - ABEA_KMER_SIZE + 1;

@@ -108,13 +108,16 @@ typedef enum {
 
 /* Execution forms.
  *  PLAIN   — the reference's structure: three kernels (pre, core, post) launched
- *            one after the other, one thread block per read, full score and
- *            trace matrices in HBM (GPU/align_cuda.c:680-850).
+ *            one after the other, one thread block per read, the backpointer
+ *            (trace) matrix in HBM (GPU/align_cuda.c:680-850); every band's
+ *            scores too only with ABEA_OPT_STORE_SCORES.
  *  BATCHED — one persistent kernel (pre, fill and traceback fused) of one
- *            block per SM: the longest reads on a 512-thread shape (their
- *            traceback walked by the whole block), the rest one warp each, first
- *            spread round-robin over the blocks, then pulled longest-first from a
- *            device queue; replayed as one CUDA graph. */
+ *            512-thread block per SM: the longest reads on the wide shape
+ *            (twelve warps: four run the band-to-band chain, eight compute the
+ *            emissions ahead of it; the traceback is walked by the whole block),
+ *            the rest one warp each, first spread round-robin over the blocks,
+ *            then pulled longest-first from a device queue; replayed as one CUDA
+ *            graph. */
 typedef enum { ABEA_MODE_PLAIN = 0, ABEA_MODE_BATCHED = 1 } abea_mode_t;
 
 /* Context options (abea_ctx_set_option). */
@@ -122,7 +125,7 @@ typedef enum {
     ABEA_OPT_MODE = 0,          /* abea_mode_t */
     ABEA_OPT_STORE_SCORES = 1,  /* 1: keep every band's scores in HBM (reference layout, GPU/align_cuda.c:573-577) */
     ABEA_OPT_USE_GRAPH = 2,     /* BATCHED only: 1 = replay the step as one CUDA graph */
-    ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide (16-warp) shape; 0 = autotuned */
+    ABEA_OPT_LONG_READ_BANDS = 3,  /* BATCHED: reads with at least this many bands use the wide shape; 0 = autotuned */
     ABEA_OPT_SPIN_LIMIT = 4,    /* upper bound on any device-side wait, in polling iterations */
     ABEA_OPT_VAR_AWARE = 5,     /* 1: emissions use level_stdv*var and level_log_stdv+log_var (the
                                    reference ignores var, GPU/align_cuda.cl:509); taken at batch creation */
@@ -232,7 +235,7 @@ abea_status_t abea_batch_timing(abea_ctx_t *ctx, abea_batch_t *batch, abea_timin
 void abea_batch_destroy(abea_batch_t *batch);
 
 /* Autotuner: runs the batched form on `batch` with several thresholds for the
- * wide (256-thread) shape and keeps the fastest for this workload's signature
+ * wide shape and keeps the fastest for this workload's signature
  * (log2 buckets of its longest read, read count and total bands); later
  * batched runs with ABEA_OPT_LONG_READ_BANDS = 0 and the same signature use it.
  * Returns the threshold (INT64_MAX = no wide reads) and its time. */
@@ -412,14 +415,21 @@ abea_status_t abea_align_stream(abea_ctx_t *ctx, const abea_stream_config_t *cfg
  * stream) and returns without waiting.  Inputs (sequence, events, model) and
  * outputs (pairs, capacity out_capacity; *n_pairs = count, 0 = failed QC,
  * negative = abea_status_t of the read) are caller-owned device-accessible
- * memory.  All scratch comes from one fixed 32 MiB device array inside this
- * library, present on every GPU that loads it until the process exits; reads
- * needing more (about 250,000 bands, n_events + n_kmers + 2) are rejected with
- * ABEA_ERR_INVALID_ARG.  No cudaMalloc or other allocation happens.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress),
- * so make it before any stream capture.  Every call uses the same array: calls
- * whose work overlaps on the GPU (other streams, other threads) race; order
- * them on one stream. */
+ * memory.  All scratch comes from one fixed 32 MiB (33,554,432-byte) device
+ * array inside this library, present on every GPU that loads it until the
+ * process exits.  A read needs, each region rounded up to 256 bytes: the read's
+ * descriptor (256), 2 regions of 4 * round16(n_events) bytes, 4 of
+ * 4 * round16(n_kmers), one of 128 * round4(n_bands) and one of
+ * 4 * round4(n_bands), plus 512 (n_kmers = sequence_len - 5, n_bands =
+ * n_events + n_kmers + 2, roundM = rounded up to a multiple of M) — about
+ * 143 bytes per band, so reads of up to about 230,000 bands fit; larger reads
+ * are rejected with ABEA_ERR_INVALID_ARG before any device work.  No cudaMalloc
+ * or other allocation happens.  The first call in each CUDA context (once per
+ * device, and again after a device reset or in a context the caller created)
+ * looks up the array's device address (cudaGetSymbolAddress), so make it
+ * before any stream capture.  Every call uses the same array: calls whose work
+ * overlaps on the GPU (other streams, other threads) race; order them on one
+ * stream. */
 abea_status_t abea_align_noalloc(abea_aligned_pair_t *pairs, int32_t *n_pairs, int32_t out_capacity,
                                  const char *sequence, int32_t sequence_len, const abea_event_t *events,
                                  int32_t n_events, const abea_model_t *model, abea_scalings_t scaling,

@@ -69,18 +69,24 @@ def test_edge_cases_match_reference(lib, oracle_mod, ref_synthetic, mode):
         assert np.array_equal(bll.view(np.int32).reshape(-1, 2), rbll), name
 
 
-@pytest.mark.parametrize("seed", [1, 2])
-def test_small_workload_bit_exact(lib, oracle_mod, seed):
+@pytest.mark.parametrize("shape", ["warp", "wide"])
+@pytest.mark.parametrize("seed", [1, 2, 4])
+def test_small_workload_bit_exact(lib, oracle_mod, seed, shape):
+    """Every score, backpointer and band origin of three reads, and every read's
+    best score, against the oracle: on the warp shape (plain form) and on the
+    wide shape (batched form with every read wide)."""
     from abea_gb300 import synth
     batch = synth.make_batch("small", seed=seed)
-    ctx = abea.Context(0, abea.MODE_PLAIN, store_scores=True)
+    ctx = abea.Context(0, abea.MODE_PLAIN if shape == "warp" else abea.MODE_BATCHED, store_scores=True)
+    if shape == "wide":
+        ctx.set_option(abea.OPT_LONG_READ_BANDS, 1)
     dev = ctx.upload(batch)
     dev.run()
     gp, gc = dev.results()
     op, oc, obest = oracle_batch(oracle_mod, batch)
     assert_same_alignments(batch, gp, gc, op, oc)
     assert np.array_equal(dev.best_scores().view(np.uint32), obest.view(np.uint32))
-    for i in (0, 7, 63):
+    for i in (0, 7, 47, 63):
         b, t, bll = dev.read_bands(i, scores=True)
         _, _, info = oracle_mod.align(batch.sequence(i), batch.read_events(i), batch.model,
                                       batch.scalings[i], want_bands=True)
