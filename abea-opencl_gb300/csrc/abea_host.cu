@@ -556,11 +556,13 @@ static int64_t d2h_bytes(const abea_batch* b) {
 //     times the warps sharing its SM in the first wave (the blocks without a
 //     wide read share the other reads round-robin, at most 16 warps each);
 //   the warp-shape work spread over those blocks, kWarpSmCyc per band per SM.
-// Calibrated on GB300 (the f5c batch, a 1,024-read batch of 1-10 kb reads and the
-// 4,096-read adjoint batch).  Ties go to fewer wide reads; the threshold is the
-// band count of the n-th wide read (none: INT64_MAX).
+// Calibrated on GB300 by sweeping the number of wide reads (the f5c batch at two
+// seeds: best 80-100 wide reads, 10.19 ms; the uneven batch: best 20-24; a
+// 1,024-read batch of 1-10 kb reads and the 4,096-read adjoint batch: best none).
+// kWarpFloorCyc includes the warp-shape read's traceback.  Ties go to fewer wide
+// reads; the threshold is the band count of the n-th wide read (none: INT64_MAX).
 static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
-    constexpr double kWideCyc = 510, kWarpFloorCyc = 1440, kWarpSmCyc = 250;
+    constexpr double kWideCyc = 400, kWarpFloorCyc = 1800, kWarpSmCyc = 250;
     const size_t n = b->order.size();
     std::vector<int64_t> wide_ok;  // band counts of the reads that may be wide, longest first
     double rest_bands = 0;
