@@ -20,14 +20,28 @@
 //    outside the kernels' band loops.
 //
 // exact_sum(a, B, c) returns RN32(RN64(RN64(a + B) + c)) for floats a, c and a
-// double B = bh + bl + r (bh = RN32(B), bl = RN32(B - bh), |r| <= 2^-48|B|):
-// TwoSum (Knuth) gives p + q = c + bh and Fast2Sum (Dekker 1971) s + e = a + p
-// exactly, the
-// exact sum a + B + c lies within eb = 2^-42 (|a| + |c| + |bh|) of s + t with
-// t = e + (q + bl) (eb also covers the reference's own two double roundings,
-// each <= 2^-53 of the same magnitudes), and RN32(s + (t + eb)) ==
-// RN32(s + (t - eb)) proves by monotonicity of rounding that the reference's
-// double result rounds to that float.
+// double B = bh + bl + r (bh = RN32(B), bl = RN32(B - bh), |r| <= 2^-48|B|).
+// Write M = |a| + |c| + |bh| and u = 2^-24 (float unit roundoff).
+//  1. TwoSum (Knuth) gives p + q = c + bh exactly (|q| <= u|p|); Fast2Sum
+//     (Dekker 1971) gives s + e = a + p exactly when |a| >= |p| (checked;
+//     |e| <= u|s|).  So the exact sum T = a + B + c = s + e + q + bl + r.
+//  2. w = RN32(q + bl) and t = RN32(e + w) round once each:
+//     |w - (q + bl)| <= u|w| <= 2u^2 M and |t - (e + w)| <= u|t| <= 4u^2 M,
+//     with |r| <= 2^-48 M, so |T - (s + t)| <= 7u^2 M < 2^-45 M.
+//  3. The reference rounds twice in double: X1 = RN64(a + B), X = RN64(X1 + c),
+//     |X - T| <= 2^-53 (|a + B| + |X1 + c|) <= 2^-51 M.  Hence
+//     |X - (s + t)| <= D with D = 2^-45 M + 2^-51 M < 2^-44 M.
+//  4. eb = RN32(RN32(|a| + |c| + ...) * 2^-42) >= 2^-42 M (1 - 2u) (the scaling
+//     by a power of two is exact).  RN32(t + eb) rounds t + eb once:
+//     RN32(t + eb) >= t + eb - u(|t| + eb) >= t + D, because |t| <= 4uM and
+//     eb (1 - u) - u|t| >= 2^-42 M (1 - 3u) - 4u^2 M > 2^-44 M >= D.
+//     Likewise RN32(t - eb) <= t - D.
+//  5. So s + RN32(t - eb) <= X <= s + RN32(t + eb) as real numbers, and by
+//     monotonicity of RN32, hm = RN32(s + RN32(t - eb)) <= RN32(X) <=
+//     hp = RN32(s + RN32(t + eb)).  hp == hm proves RN32(X) == hp: the
+//     reference's double result rounds to that float.  The margin is a factor
+//     4 or more (eb >= 4D), so the check declines only within a few 2^-42 M of
+//     a float rounding boundary.
 //
 // All float arithmetic goes through __f*_rn intrinsics so nvcc never contracts
 // it into FMAs (the library is also built with -fmad=false); the only FMAs are

@@ -447,6 +447,7 @@ typedef struct {
     const int32_t *order;
     int next;
     pthread_mutex_t lock;
+    double *best_f64;  /* non-NULL: the all-FP64 twin (oracle_align_f64) */
 } batch_job_t;
 
 static void *batch_worker(void *arg) {
@@ -460,6 +461,13 @@ static void *batch_worker(void *arg) {
         oracle_debug_t dbg;
         memset(&dbg, 0, sizeof(dbg));
         int32_t ne = job->n_events[i];
+        if (job->best_f64) {
+            job->out_n[i] = oracle_align_f64(job->out_pairs + 2 * job->event_ptr[i], 2 * ne,
+                                             job->read + job->read_ptr[i], job->read_len[i],
+                                             job->event_table + job->event_ptr[i], ne, job->model,
+                                             job->scalings[i], job->flags, &job->best_f64[i]);
+            continue;
+        }
         job->out_n[i] = oracle_align(job->out_pairs + 2 * job->event_ptr[i], 2 * ne,
                                      job->read + job->read_ptr[i], job->read_len[i],
                                      job->event_table + job->event_ptr[i], ne, job->model,
@@ -476,12 +484,39 @@ static int cmp_desc(const void *a, const void *b) {
     return *(const int32_t *)a - *(const int32_t *)b;
 }
 
+static void run_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
+                      const int32_t *read_len, const abea_event_t *event_table,
+                      const int64_t *event_ptr, const int32_t *n_events,
+                      const abea_scalings_t *scalings, const abea_model_t *model,
+                      abea_aligned_pair_t *out_pairs, int32_t *out_n, float *best_scores,
+                      double *best_f64, uint32_t flags, int n_threads);
+
 void oracle_align_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
                         const int32_t *read_len, const abea_event_t *event_table,
                         const int64_t *event_ptr, const int32_t *n_events,
                         const abea_scalings_t *scalings, const abea_model_t *model,
                         abea_aligned_pair_t *out_pairs, int32_t *out_n, float *best_scores,
                         uint32_t flags, int n_threads) {
+    run_batch(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model,
+              out_pairs, out_n, best_scores, NULL, flags, n_threads);
+}
+
+void oracle_align_f64_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
+                            const int32_t *read_len, const abea_event_t *event_table,
+                            const int64_t *event_ptr, const int32_t *n_events,
+                            const abea_scalings_t *scalings, const abea_model_t *model,
+                            abea_aligned_pair_t *out_pairs, int32_t *out_n, double *best_scores,
+                            uint32_t flags, int n_threads) {
+    run_batch(n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events, scalings, model,
+              out_pairs, out_n, NULL, best_scores, flags, n_threads);
+}
+
+static void run_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
+                      const int32_t *read_len, const abea_event_t *event_table,
+                      const int64_t *event_ptr, const int32_t *n_events,
+                      const abea_scalings_t *scalings, const abea_model_t *model,
+                      abea_aligned_pair_t *out_pairs, int32_t *out_n, float *best_scores,
+                      double *best_f64, uint32_t flags, int n_threads) {
     if (n_reads <= 0) return;
     if (n_threads < 1) n_threads = 1;
     int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)n_reads);
@@ -498,7 +533,7 @@ void oracle_align_batch(int32_t n_reads, const char *read, const int64_t *read_p
 
     batch_job_t job = {n_reads, read, read_ptr, read_len, event_table, event_ptr, n_events,
                        scalings, model, out_pairs, out_n, best_scores, flags, order, 0,
-                       PTHREAD_MUTEX_INITIALIZER};
+                       PTHREAD_MUTEX_INITIALIZER, best_f64};
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)n_threads);
     int started = 0;
     for (int t = 0; t < n_threads; ++t)

@@ -67,6 +67,14 @@ int32_t oracle_align_f64(abea_aligned_pair_t *out, int32_t out_cap, const char *
                          int32_t seq_len, const abea_event_t *events, int32_t n_events,
                          const abea_model_t *model, abea_scalings_t scaling, uint32_t flags,
                          double *best_score);
+/* The FP64 twin over a flattened batch on n_threads threads (longest read first);
+ * best_scores[i] = the read's FP64 best-end score (-inf when none is finite). */
+void oracle_align_f64_batch(int32_t n_reads, const char *read, const int64_t *read_ptr,
+                            const int32_t *read_len, const abea_event_t *event_table,
+                            const int64_t *event_ptr, const int32_t *n_events,
+                            const abea_scalings_t *scalings, const abea_model_t *model,
+                            abea_aligned_pair_t *out_pairs, int32_t *out_n, double *best_scores,
+                            uint32_t flags, int n_threads);
 
 /* The reference emission, float arithmetic in the reference's order
  * (GPU/align_cuda.cl:85-110, align_swi.cl:77-111). */

@@ -70,6 +70,8 @@ def lib():
                                        C.POINTER(C.c_double)]
         L.oracle_align_batch.restype = None
         L.oracle_align_batch.argtypes = [C.c_int32] + [C.c_void_p] * 11 + [C.c_uint32, C.c_int]
+        L.oracle_align_f64_batch.restype = None
+        L.oracle_align_f64_batch.argtypes = [C.c_int32] + [C.c_void_p] * 11 + [C.c_uint32, C.c_int]
         L.oracle_emission.restype = C.c_float
         L.oracle_emission.argtypes = [C.c_float, C.c_void_p, _Scalings, C.c_uint32]
         L.oracle_add3.restype = C.c_float
@@ -157,6 +159,48 @@ def align_batch(batch, flags: int = 0, threads: int | None = None):
     L.oracle_align_batch(n, *[_ptr(a) for a in arrs], _ptr(pairs), _ptr(counts), _ptr(best),
                          flags, threads or os.cpu_count() or 1)
     return pairs, counts, best
+
+
+def align_batch_f64(batch, flags: int = 0, threads: int | None = None):
+    """The all-FP64 recurrence (oracle_align_f64) over a flattened batch; returns
+    (pairs, counts, best_scores as float64)."""
+    L = lib()
+    n = batch.n_reads
+    pairs = np.zeros(max(batch.pair_capacity(), 1), dtype=PAIR_DTYPE)
+    counts = np.zeros(n, dtype=np.int32)
+    best = np.zeros(n, dtype=np.float64)
+    arrs = [np.ascontiguousarray(a) for a in (
+        batch.read, batch.read_ptr.astype(np.int64), batch.read_len.astype(np.int32),
+        np.asarray(batch.events, dtype=EVENT_DTYPE), batch.event_ptr.astype(np.int64),
+        batch.n_events.astype(np.int32), np.asarray(batch.scalings, dtype=SCALINGS_DTYPE),
+        np.asarray(batch.model, dtype=MODEL_DTYPE))]
+    L.oracle_align_f64_batch(n, *[_ptr(a) for a in arrs], _ptr(pairs), _ptr(counts), _ptr(best),
+                             flags, threads or os.cpu_count() or 1)
+    return pairs, counts, best
+
+
+def fp64_error(batch, best32, pairs32, counts32, threads: int | None = None) -> dict:
+    """How far the reference's FP32 results lie from the all-FP64 recurrence on
+    the same inputs: relative error of the best-end scores (reads with a finite
+    end in both), and the reads whose AlignedPairs or pair counts differ."""
+    p64, c64, b64 = align_batch_f64(batch, threads=threads)
+    b32 = np.asarray(best32, dtype=np.float64)
+    fin = np.isfinite(b32) & np.isfinite(b64)
+    rel = np.abs(b32[fin] - b64[fin]) / np.maximum(np.abs(b64[fin]), 1e-300)
+    diff_counts = int(np.count_nonzero(np.asarray(counts32) != c64))
+    diff_pairs = 0
+    for i in range(batch.n_reads):
+        o, n32, n64 = 2 * int(batch.event_ptr[i]), int(counts32[i]), int(c64[i])
+        if n32 != n64 or (n32 > 0 and not np.array_equal(pairs32[o:o + n32], p64[o:o + n64])):
+            diff_pairs += 1
+    return {"reads": int(batch.n_reads), "finite_ends": int(fin.sum()),
+            "best_score_rel_err_max": float(rel.max()) if rel.size else 0.0,
+            "best_score_rel_err_median": float(np.median(rel)) if rel.size else 0.0,
+            "best_score_rel_err_p99": float(np.percentile(rel, 99)) if rel.size else 0.0,
+            "reads_with_other_pair_count": diff_counts,
+            "reads_with_other_pairs": diff_pairs,
+            "reads_passing_qc_fp32": int(np.count_nonzero(np.asarray(counts32) > 0)),
+            "reads_passing_qc_fp64": int(np.count_nonzero(c64 > 0))}
 
 
 def emission(x: float, model_entry, scalings, flags: int = 0) -> float:

@@ -181,14 +181,49 @@ def test_exact_arithmetic_selftest(lib):
     assert 2 * r["cases"] - r["sum_declined"] > r["cases"]
 
 
+@pytest.mark.parametrize("workload", ["f5c_batch", "uneven"])
 @pytest.mark.parametrize("mode", [abea.MODE_PLAIN, abea.MODE_BATCHED])
-def test_f5c_batch_full_size(lib, oracle_mod, mode):
-    """The whole benchmark workload (1.3 Mbases, ~360 reads), bit-exact."""
+def test_benchmark_batches_full_size(lib, oracle_mod, mode, workload):
+    """The two benchmarked 1.3 Mbase batches exactly as the benchmark builds them
+    (seed 1): the f5c batch (~360 reads) and the heavy-tailed uneven batch (reads
+    up to 100 kb): AlignedPairs and best-end scores bit-exact with the oracle."""
     from abea_gb300 import synth
-    batch = synth.make_batch("f5c_batch", seed=1)
-    _, gp, gc = run(batch, mode)
-    op, oc, _ = oracle_batch(oracle_mod, batch)
+    batch = synth.make_batch(workload, seed=1)
+    ctx = abea.Context(0, mode)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    op, oc, obest = oracle_batch(oracle_mod, batch)
     assert_same_alignments(batch, gp, gc, op, oc)
+    assert np.array_equal(dev.best_scores().view(np.uint32), obest.view(np.uint32))
+
+
+# Relative error of the FP32 best-end scores against the all-FP64 recurrence,
+# measured on these batches (seed 1): small 3.4e-6, f5c 5.5e-6, uneven 2.3e-5 (the
+# error grows with read length: 100 kb reads).  The bounds leave a factor ~2.
+FP64_REL_BOUND = {"small": 1e-5, "f5c_batch": 1e-5, "uneven": 5e-5}
+
+
+@pytest.mark.parametrize("workload", ["small", "f5c_batch", "uneven"])
+def test_error_against_fp64_is_bounded(lib, oracle_mod, workload):
+    """The GPU's best scores are the reference's FP32 results bit for bit; their
+    distance to the all-FP64 recurrence (the oracle's FP64 twin) is stated and
+    bounded, and only a few reads take other AlignedPairs under FP64."""
+    from abea_gb300 import synth
+    batch = synth.make_batch(workload, seed=1)
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    best = dev.best_scores()
+    _, _, obest = oracle_batch(oracle_mod, batch)
+    assert np.array_equal(best.view(np.uint32), obest.view(np.uint32))
+    e = oracle_mod.fp64_error(batch, best, gp, gc, threads=os.cpu_count())
+    print(workload, e)
+    assert e["finite_ends"] == batch.n_reads
+    assert e["best_score_rel_err_max"] < FP64_REL_BOUND[workload]
+    assert e["reads_with_other_pair_count"] == 0
+    assert e["reads_with_other_pairs"] <= max(3, batch.n_reads // 20)
 
 
 def test_uneven_batch_batched_equals_plain(lib):
