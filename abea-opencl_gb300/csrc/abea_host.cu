@@ -1302,8 +1302,8 @@ extern "C" int32_t abea_internal_stage_db(int32_t n_reads, char* const* read, co
     const size_t n = (size_t)n_reads;
     std::vector<int64_t> read_ptr(n), event_ptr(n);
     int64_t seq_bytes = 0, events = 0;
-    for (size_t i = 0; i < n; ++i) {
-        if (read_len[i] < 0) return -1;
+    for (size_t i = 0; i < n; ++i) {  // the same per-read checks as abea_align_db
+        if (read_len[i] < 0 || (read_len[i] > 0 && !read[i]) || (et[i].n > 0 && !et[i].event)) return -1;
         read_ptr[i] = seq_bytes;
         seq_bytes += read_len[i] + 1;
         event_ptr[i] = events;

@@ -2500,6 +2500,11 @@ __global__ void __launch_bounds__(128) abea_postalign_kernel(PostalignArgs a) {
         }
         return;
     }
+    // Pass 1 above accepted only paths whose every step moves the k-mer and the
+    // event forward by 0 or 1 (not both 0): the events are non-decreasing along
+    // the path, so its first and last pairs hold the smallest and largest event
+    // (the oracle takes the minimum and maximum; a path that is not monotone
+    // never gets here, it is ABEA_ERR_INTERNAL).
     const int e_first = P[0].read_pos, e_last = P[n - 1].read_pos;
     const char* s = a.seq + r.seq_off;
     abea_index_pair_t* map = a.map + r.seq_off;

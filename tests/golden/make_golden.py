@@ -10,9 +10,9 @@
                          compiled by oracle/build_ref.sh; full band matrices are kept
                          for the smallest ones.
 
-Run from the repository root in a checkout that has the reference at
-$ABEA_REFERENCE_DIR (default /root/reference):
-    python tests/golden/make_golden.py
+Run from the repository root with the reference checkout named by
+$ABEA_REFERENCE_DIR (required):
+    ABEA_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -24,7 +24,9 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("ABEA_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("ABEA_REFERENCE_DIR", "")
+if not REF:
+    sys.exit("make_golden.py: set ABEA_REFERENCE_DIR to the reference checkout")
 OUT = os.path.dirname(os.path.abspath(__file__))
 DUMP_READS = [51, 125, 101, 70, 57, 133]
 

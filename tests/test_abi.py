@@ -79,3 +79,32 @@ def test_argument_checks_without_device(libpath):
     f.restype = C.c_int32
     assert f(-1, None, None, None, None, None, 0) == -1
     assert f(0, None, None, None, None, None, 0) == 0
+
+
+def test_staging_refuses_null_per_read_arrays(libpath):
+    """abea_internal_stage_db checks each read as abea_align_db does: a read with
+    bases but no sequence pointer, or events but no event pointer, is refused
+    (-1) before any copy."""
+    import ctypes as C
+    import numpy as np
+    L = abea.lib()
+    vp = C.c_void_p
+    f = L.abea_internal_stage_db
+    f.argtypes = [C.c_int32] + [vp] * 5 + [C.c_int32]
+    f.restype = C.c_int32
+
+    class ET(C.Structure):
+        _fields_ = [("n", C.c_size_t), ("start", C.c_size_t), ("end", C.c_size_t), ("event", C.c_void_p)]
+    seq = np.zeros(64, dtype=np.uint8)
+    ev = np.zeros(64 * 24, dtype=np.uint8)
+    good = np.frombuffer(b"ACGTACGTAC\0", dtype=np.uint8).copy()
+    evs = np.zeros(3 * 24, dtype=np.uint8)
+    lens = np.array([10], dtype=np.int32)
+    et = (ET * 1)()
+    et[0].n, et[0].start, et[0].end, et[0].event = 3, 0, 3, evs.ctypes.data
+    reads = (C.c_void_p * 1)(good.ctypes.data)
+    assert f(1, reads, lens.ctypes.data, C.cast(et, vp), seq.ctypes.data, ev.ctypes.data, 1) == 0
+    no_read = (C.c_void_p * 1)(None)
+    assert f(1, no_read, lens.ctypes.data, C.cast(et, vp), seq.ctypes.data, ev.ctypes.data, 1) == -1
+    et[0].event = None
+    assert f(1, reads, lens.ctypes.data, C.cast(et, vp), seq.ctypes.data, ev.ctypes.data, 1) == -1

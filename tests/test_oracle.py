@@ -6,8 +6,17 @@ import pytest
 
 from conftest import ROOT
 
-REF_DUMP = os.path.join(os.environ.get("ABEA_REFERENCE_DIR", "/root/reference"),
-                        "FPGA/code/bins/dump_small/0")
+def _reference_dir():
+    """ABEA_REFERENCE_DIR, else the checkout oracle/build_ref.sh compiled from ("" when none)."""
+    d = os.environ.get("ABEA_REFERENCE_DIR", "")
+    rec = os.path.join(ROOT, "oracle", "_ref", "source_dir")
+    if not d and os.path.exists(rec):
+        with open(rec) as f:
+            d = f.read().strip()
+    return d
+
+
+REF_DUMP = os.path.join(_reference_dir(), "FPGA/code/bins/dump_small/0") if _reference_dir() else ""
 
 
 def test_oracle_dump_subset_bit_exact(oracle_mod, dump_subset):
@@ -22,7 +31,7 @@ def test_oracle_dump_subset_bit_exact(oracle_mod, dump_subset):
             assert np.array_equal(got[i], g), f"read {i} flags {flags}"
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_DUMP), reason="reference checkout not present")
+@pytest.mark.skipif(not REF_DUMP or not os.path.isdir(REF_DUMP), reason="reference checkout not present")
 def test_oracle_full_dump_bit_exact(oracle_mod):
     """All 143 reads / 1,461,052 pairs of the reference's golden dump."""
     from abea_gb300 import dump
