@@ -463,10 +463,25 @@ def selftest_arith(cases: int = 1 << 26, seed: int = 1) -> dict:
                 sum_declined=int(out[3]), cases=int(out[4]))
 
 
+def heuristic_wide_reads(n_bands, blocks: int) -> int:
+    """How many of the longest reads the batched form runs on the wide shape when
+    left to its own heuristic, for a batch with these band counts on `blocks`
+    resident blocks (one per SM).  Host code only (abea_internal_wide_threshold)."""
+    L = lib()
+    f = L.abea_internal_wide_threshold
+    f.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    f.restype = C.c_int64
+    b = np.ascontiguousarray(n_bands, dtype=np.int64)
+    thr = f(b.ctypes.data, len(b), int(blocks))
+    if thr < 0:
+        raise AbeaError(-1, "abea_internal_wide_threshold: bad argument")
+    return 0 if thr >= 2**62 else int(min(np.sum(b >= thr), blocks))
+
+
 def version() -> str:
     return lib().abea_version().decode()
 
 
 __all__ = ["align", "Context", "DeviceBatch", "Batch", "from_reads", "split_pairs", "split_postalign", "build", "lib",
            "AbeaError", "MODE_PLAIN", "MODE_BATCHED", "types", "EXPORTS", "version",
-           "selftest_arith", "pinned_empty", "pin_batch", "StreamConfig", "StreamStats"]
+           "selftest_arith", "pinned_empty", "pin_batch", "StreamConfig", "StreamStats", "heuristic_wide_reads"]

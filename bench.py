@@ -8,9 +8,14 @@ One step = one pass of pre/core/post over the whole synthetic batch (1.3 Mbases,
 lognormal read lengths, median 3 kb, clipped 500 b - 20 kb), inputs resident in
 HBM, L2 flushed before every timed step.  `e2e` is the same metric through
 abea_align_batch with pinned host buffers (host->device and device->host copies
-inside the timed region).  Under torchrun every rank aligns its own shard of the
-reads (longest-processing-time partition by band cells, no collective on the data
-path; weak scaling) and rank 0 prints one JSON line.
+inside the timed region).  The headline uses the library's own choice of wide
+reads (its heuristic); the autotuner's choices are reported beside it.
+
+Several GPUs: `--gpus N` starts N ranks (one process per GPU) unless the caller
+already did (torchrun sets WORLD_SIZE).  Reads are independent, so the path
+shards with no collective on the data path: every rank aligns its own batch of
+the same shape (seed + rank; weak scaling); the ranks meet only for the timing
+maximum and the totals.
 """
 from __future__ import annotations
 
@@ -51,39 +56,83 @@ WORKLOADS = {
 
 # ---------------------------------------------------------------- distributed helpers
 class Dist:
-    def __init__(self):
+    """Rank / world from the launcher's environment; a process group only for
+    the timing maximum and the totals (NCCL between GPUs, gloo otherwise)."""
+
+    def __init__(self, use_cuda: bool, init: bool = True):
         self.rank = int(os.environ.get("RANK", "0"))
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
-        if self.world > 1:
+        self.device = None
+        if self.world > 1 and init:
+            import torch
             import torch.distributed as dist
-            dist.init_process_group("gloo")
+            if use_cuda:
+                torch.cuda.set_device(self.local_rank)
+                self.device = torch.device("cuda", self.local_rank)
+            dist.init_process_group("nccl" if use_cuda else "gloo")
             self.pg = dist
+
+    def _reduce(self, v: float, op) -> float:
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
+        self.pg.all_reduce(t, op=op)
+        return float(t.item())
 
     def barrier(self):
         if self.pg:
-            self.pg.barrier()
+            self._reduce(0.0, self.pg.ReduceOp.SUM)
 
     def max(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
-        return float(t.item())
+        return self._reduce(v, self.pg.ReduceOp.MAX) if self.pg else v
 
     def sum(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
-        return float(t.item())
+        return self._reduce(v, self.pg.ReduceOp.SUM) if self.pg else v
 
     def close(self):
         if self.pg:
             self.pg.destroy_process_group()
+
+
+def visible_gpus() -> int:
+    """GPUs this process may use: nvidia-smi's list, cut by CUDA_VISIBLE_DEVICES."""
+    try:
+        out = subprocess.run(["nvidia-smi", "-L"], capture_output=True, text=True, timeout=60).stdout
+    except (OSError, subprocess.SubprocessError):
+        return 0
+    n = sum(1 for line in out.splitlines() if line.startswith("GPU "))
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if cvd is not None:
+        n = min(n, len([x for x in cvd.split(",") if x.strip()]))
+    return n
+
+
+def rank_env(rank: int, world: int, port: int) -> dict:
+    env = dict(os.environ)
+    env.update({"RANK": str(rank), "LOCAL_RANK": str(rank), "WORLD_SIZE": str(world),
+                "LOCAL_WORLD_SIZE": str(world), "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    return env
+
+
+def launch_ranks(args) -> int:
+    """`--gpus N` without a launcher: one process per GPU (rank r on GPU r), this
+    same command line, rendezvous on 127.0.0.1.  Refuses more GPUs than are
+    visible (the reference arm runs on the host and needs none)."""
+    n = args.gpus
+    if args.impl == "ours":
+        have = visible_gpus()
+        if n > have:
+            print(f"bench.py: --gpus {n} but {have} GPU(s) are visible", file=sys.stderr)
+            return 2
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, os.path.abspath(__file__)] + sys.argv[1:]
+    procs = [subprocess.Popen(cmd, env=rank_env(r, n, port)) for r in range(n)]
+    rcs = [p.wait() for p in procs]
+    return next((rc for rc in rcs if rc != 0), 0)
 
 
 # ---------------------------------------------------------------- clocks
@@ -175,6 +224,8 @@ def reference_arm(args, dist):
     """The reference's CPU align() path on the host cores (the oracle port of
     align_swi.cl + align_swi.cpp; the reference's own code when it compiled here)."""
     if dist.rank != 0:
+        print(f"bench.py: rank {dist.rank}/{dist.world} exits without work (the reference arm runs on rank 0)",
+              file=sys.stderr, flush=True)
         return 0
     pkg = load_package()
     from abea_gb300 import synth
@@ -196,7 +247,7 @@ def reference_arm(args, dist):
         "dtype": "f32 scores, f64 transition adds", "data": "synthetic",
         "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload),
                    "reads": batch.n_reads, "band_cells": cells, "seed": args.seed},
-        "reads_per_s": batch.n_reads / t,
+        "reads_per_s": batch.n_reads / t, "n_ranks": dist.world,
         "cpu_baseline": {"value": v, "unit": "band-cells/s", "cores": threads, "kind": kind,
                          "sample": f"the whole {args.workload} batch per step"},
         "e2e": {"value": v, "unit": "band-cells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -443,14 +494,90 @@ def serving_report(pkg, synth, device, seed, mbases: float):
     }
 
 
+def longest_read_ms(pkg, batch, device):
+    """The batch's longest read alone on the wide shape (batched form, one read):
+    the step can be no shorter than this (a read's bands run in sequence)."""
+    i = int(np.argmax(batch.n_bands()))
+    one = batch.subset(np.array([i]))
+    ctx = pkg.Context(device, pkg.MODE_BATCHED)
+    ctx.set_option(pkg.OPT_LONG_READ_BANDS, 1)
+    dev = ctx.upload(one)
+    dev.run()
+    dev.sync()
+    ts = []
+    for _ in range(3):
+        ctx.flush_l2()
+        ctx.mark(0)
+        dev.run()
+        ctx.mark(1)
+        ts.append(ctx.elapsed(0, 1))
+    dev.close()
+    ctx.close()
+    return min(ts), int(one.n_bands()[0])
+
+
+def autotune_report(pkg, synth, batch, args, device):
+    """The autotuner beside the heuristic headline: a threshold tuned on another
+    batch of the same shape (seed + 100) and set on this one's context, and one
+    tuned on this very batch."""
+    other = synth.make_batch(args.workload, seed=args.seed + 100)
+    ctx = pkg.Context(device, pkg.MODE_BATCHED)
+    d2 = ctx.upload(other)
+    thr_other, _ = d2.autotune()
+    d2.close()
+    dev = ctx.upload(batch)
+    ctx.set_option(pkg.OPT_LONG_READ_BANDS, int(thr_other))
+    ms_other = statistics.mean(time_device(pkg, ctx, dev, 5, 1)[0])
+    ctx.set_option(pkg.OPT_LONG_READ_BANDS, 0)
+    thr_self, _ = dev.autotune()
+    ms_self = statistics.mean(time_device(pkg, ctx, dev, 5, 1)[0])
+    nb = batch.n_bands()
+    dev.close()
+    ctx.close()
+    return {"tuned_on_other_seed": {"seed": args.seed + 100, "threshold_bands": int(thr_other),
+                                    "wide_reads": int((nb >= thr_other).sum()), "ms_per_step": ms_other},
+            "tuned_on_this_batch": {"threshold_bands": int(thr_self), "wide_reads": int((nb >= thr_self).sum()),
+                                    "ms_per_step": ms_self}}
+
+
+def align_threads_report(pkg, batch, threads: int = 8, max_reads: int = 256):
+    """f5c's calling pattern: align() once per read from `threads` host threads at
+    once (each thread its own context and stream inside the library), on the
+    batch's reads; reads/s, and the results against one batched run."""
+    import concurrent.futures as cf
+    n = min(batch.n_reads, max_reads)
+    idx = list(range(n))
+    seqs = [batch.sequence(i) for i in idx]
+    evs = [np.ascontiguousarray(batch.read_events(i)) for i in idx]
+
+    def one(i):
+        return pkg.align(seqs[i], evs[i], batch.model, batch.scalings[i])
+    with cf.ThreadPoolExecutor(threads) as ex:  # warm-up: each thread's context
+        list(ex.map(one, idx[:threads]))
+        t0 = time.perf_counter()
+        got = list(ex.map(one, idx))
+        dt = time.perf_counter() - t0
+    ctx = pkg.Context(0, pkg.MODE_BATCHED)
+    sub = batch.subset(np.array(idx))
+    pairs, counts = ctx.align_batch(sub)
+    ctx.close()
+    ref = pkg.split_pairs(sub, pairs, counts)
+    same = all(np.array_equal(got[i], ref[i]) for i in range(n))
+    cells = sub.band_cells()
+    return {"host_threads": threads, "reads": n, "wall_s": dt, "reads_per_s": n / dt,
+            "band_cells_per_s": cells / dt, "identical_to_batched": bool(same),
+            "per_thread_device_footprint": "one context per calling thread (a stream, 24 CUDA events) and a "
+                                           "device slab grown to that thread's largest read so far: about 132 B "
+                                           "per band + 48 B per event + 17 B per base, plus 136 KB fixed "
+                                           "(a 20 kb read: ~9 MB)"}
+
+
 def ours(args, dist):
     pkg = load_package()
     from abea_gb300 import synth
     device = dist.local_rank
-    from abea_gb300.shard import shard_reads
-    full = synth.make_batch(args.workload, seed=args.seed)
-    shard = shard_reads(full.n_bands(), dist.world, dist.rank) if dist.world > 1 else np.arange(full.n_reads)
-    batch = full.subset(shard) if dist.world > 1 else full
+    # weak scaling: every rank aligns its own batch of the workload's shape
+    batch = synth.make_batch(args.workload, seed=args.seed + dist.rank)
     cells = batch.band_cells()
     mode = pkg.MODE_BATCHED if args.mode == "batched" else pkg.MODE_PLAIN
 
@@ -458,9 +585,6 @@ def ours(args, dist):
     clocks.start()  # nvidia-smi starts sampling during the setup; the summary keeps the timed region
     ctx = pkg.Context(device, mode)
     dev = ctx.upload(batch)
-    tuned = None
-    if mode == pkg.MODE_BATCHED and args.autotune:
-        tuned = dev.autotune()  # untimed: picks the wide-shape threshold for this workload
     launches_per_step = None
     for _ in range(args.warmup):
         dev.run()
@@ -481,6 +605,8 @@ def ours(args, dist):
     wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
     slow = dev.slow_cells()
+    best = dev.best_scores()
+    gpairs, gcounts = dev.results()
     dev.close()
     local_ms = sum(per_step)
     dist.barrier()
@@ -497,6 +623,11 @@ def ours(args, dist):
 
     if dist.rank != 0:
         return 0
+    nb = batch.n_bands()
+    n_wide = None
+    if mode == pkg.MODE_BATCHED:
+        import torch
+        n_wide = pkg.heuristic_wide_reads(nb, torch.cuda.get_device_properties(device).multi_processor_count)
     out = {
         "metric": "ABEA band-cells/s (f5c align, adaptive band 100)",
         "value": value, "unit": "band-cells/s", "n_gpus": dist.world, "steps": args.steps,
@@ -505,9 +636,10 @@ def ours(args, dist):
         "data": "synthetic",
         "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload),
                    "reads": int(total_reads), "band_cells": int(total_cells), "seed": args.seed,
-                   "mode": args.mode, "parallelism": f"reads sharded over {dist.world} GPU(s)",
-                   "autotuned_wide_threshold_bands": None if tuned is None else tuned[0],
                    "l2": "flushed (write of 2x L2) before every timed step"},
+        "mode": args.mode,
+        "parallelism": f"{dist.world} rank(s), one GPU each; rank r aligns its own batch (seed {args.seed} + r)",
+        "wide_reads": n_wide, "wide_threshold": "the library's heuristic (no autotuning)",
         "reads_per_s": total_reads / (ms_per_step / 1e3),
         "gpu_launches": int(launches_per_step or 0) * args.steps,
         "wall_s_timed_region": wall,
@@ -517,7 +649,7 @@ def ours(args, dist):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                 "stage_ms": {k: round(v, 4) for k, v in e2e_timing.items() if k.endswith("_ms")}},
     }
-    # roofline of the dominant kernel (core), algorithmic bytes = 5 B per band cell
+    # roofline of the dominant kernel (the fused fill + traceback), algorithmic bytes = 5 B per band cell
     peak, peak_kind = measured_peak_hbm()
     core_ms = statistics.mean(core)
     achieved = BYTES_PER_CELL * cells / (core_ms / 1e3) / 1e9
@@ -525,11 +657,27 @@ def ours(args, dist):
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": achieved / peak, "peak_kind": f"{peak_kind} (hbm_gbs)",
                        "traffic": (tpc * cells) if tpc else None,
-                       "kernel": "abea_core (fill)", "core_ms": core_ms,
+                       "kernel": "abea_batched_kernel (fill + traceback)", "core_ms": core_ms,
                        "algorithmic_bytes": BYTES_PER_CELL * cells}
     if tinfo:
         out["roofline"]["traffic_source"] = tinfo.get("source")
+    if dist.world == 1:
+        # the two bounds that do apply: the longest read's band chain, and instruction issue
+        lr_ms, lr_bands = longest_read_ms(pkg, batch, device)
+        mhz = clk.get("sm_mhz") or 2070.0
+        out["roofline"]["latency_bound"] = {
+            "longest_read_bands": lr_bands, "longest_read_alone_ms": lr_ms,
+            "frac": lr_ms / core_ms, "cycles_per_band": lr_ms * 1e-3 * mhz * 1e6 / lr_bands,
+            "note": "the longest read's bands run in sequence: the step can be no shorter than that read alone"}
+        if tinfo and tinfo.get("inst_executed_per_launch") and tinfo.get("sm_count"):
+            slots = tinfo["sm_count"] * 4 * mhz * 1e6 * core_ms * 1e-3
+            out["roofline"]["issue_bound"] = {
+                "warp_instructions_per_launch": tinfo["inst_executed_per_launch"],
+                "issue_slots": slots, "frac": tinfo["inst_executed_per_launch"] / slots,
+                "source": tinfo.get("source"),
+                "note": "warp-instructions of one launch (ncu) over the SMs' issue slots in the live step time"}
     if args.compare and dist.world == 1:
+        out["autotune"] = autotune_report(pkg, synth, batch, args, device)
         other = "plain" if args.mode == "batched" else "batched"
         om = pkg.MODE_PLAIN if other == "plain" else pkg.MODE_BATCHED
         r = run_mode(pkg, batch, om, device, max(2, args.steps // 2), 1)
@@ -539,7 +687,7 @@ def ours(args, dist):
         ub = synth.make_batch("uneven", seed=args.seed)
         un = {}
         for name, m in (("batched", pkg.MODE_BATCHED), ("plain", pkg.MODE_PLAIN)):
-            r = run_mode(pkg, ub, m, device, 2, 1, autotune=args.autotune)
+            r = run_mode(pkg, ub, m, device, 2, 1)
             ms = statistics.mean(r["per_step"])
             un[name] = {"value": ub.band_cells() / (ms / 1e3), "ms_per_step": ms}
         un["batched_over_plain"] = un["batched"]["value"] / un["plain"]["value"]
@@ -559,7 +707,7 @@ def ours(args, dist):
                 elif wl == "uneven":
                     ms = un[name]["ms_per_step"]
                 else:
-                    ms = statistics.mean(run_mode(pkg, wb, m, device, 3, 1, autotune=args.autotune)["per_step"])
+                    ms = statistics.mean(run_mode(pkg, wb, m, device, 3, 1)["per_step"])
                 row[name] = {"band_cells_per_s": wc / (ms / 1e3), "reads_per_s": wr / (ms / 1e3), "ms": ms}
             if args.cpu:
                 threads = os.cpu_count() or 1
@@ -567,6 +715,7 @@ def ours(args, dist):
                 row["cpu"] = {"band_cells_per_s": wc / t, "reads_per_s": wr / t, "ms": t * 1e3, "cores": threads}
             per[wl] = row
         out["per_config"] = per
+        out["align_threads"] = align_threads_report(pkg, batch)
     if args.compare and dist.world == 1:
         out["adjoint"] = adjoint_report(pkg, synth, device, args.seed)
         out["next_rows"] = next_rows_report(pkg, synth, device, args.seed, args.cpu)
@@ -577,8 +726,34 @@ def ours(args, dist):
         t = cpu_align(batch, threads)
         out["cpu_baseline"] = {"value": cells / t, "unit": "band-cells/s", "cores": threads, "kind": "port",
                                "sample": f"the whole {args.workload} batch, once"}
+        out["fp64_error"] = fp64_report(pkg, synth, args, batch, best, gpairs, gcounts, device)
     print(json.dumps(out), flush=True)
     return 0
+
+
+def fp64_report(pkg, synth, args, batch, best, pairs, counts, device):
+    """The checker beside the measurement: each result's distance to the all-FP64
+    recurrence (the oracle's FP64 twin on the host cores), for the GPU's own
+    best scores and AlignedPairs of the timed batch and of the small and uneven
+    batches.  The GPU's FP32 results equal the reference's FP32 arithmetic bit
+    for bit (tests/test_gpu_parity.py)."""
+    from oracle import oracle
+    res = {args.workload: oracle.fp64_error(batch, best, pairs, counts)}
+    for wl in ("small", "f5c_batch", "uneven"):
+        if wl in res:
+            continue
+        b = synth.make_batch(wl, seed=args.seed)
+        ctx = pkg.Context(device, pkg.MODE_BATCHED)
+        dev = ctx.upload(b)
+        dev.run()
+        p, c = dev.results()
+        bs = dev.best_scores()
+        dev.close()
+        ctx.close()
+        res[wl] = oracle.fp64_error(b, bs, p, c)
+    res["note"] = ("relative error of the FP32 best-end scores against the FP64 recurrence (reads with a finite "
+                   "end), and the reads whose AlignedPairs differ under FP64; the error grows with read length")
+    return res
 
 
 def main():
@@ -592,11 +767,12 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-compare", dest="compare", action="store_false")
     ap.add_argument("--no-cpu", dest="cpu", action="store_false")
-    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--serving-mbases", type=float, default=200.0,
                     help="size of the serving-stream report (0 = skip it)")
     args = ap.parse_args()
-    dist = Dist()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return launch_ranks(args)
+    dist = Dist(use_cuda=args.impl == "ours", init=args.impl == "ours")
     try:
         rc = reference_arm(args, dist) if args.impl == "reference" else ours(args, dist)
     finally:
