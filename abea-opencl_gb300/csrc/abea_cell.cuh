@@ -48,6 +48,7 @@
 // the explicit ones of the division.
 #pragma once
 #include <cuda_runtime.h>
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 
@@ -145,16 +146,21 @@ __device__ __forceinline__ float exact_sum(float a, float bh, float bl, float c,
 // equal roundings of the bracket +-eb, eb = 2^-42 (|a| + |bh|), prove the result
 // as in exact_sum.  a = -inf gives -inf (proven); otherwise ok = false when not
 // proven, which happens only while |a| < |bh| (a read's first bands).
+//
+// a = -inf (a cell outside the band, or not reached): the error terms are taken
+// from ac = max(a, -FLT_MAX), which equals a for every finite a; s = a + bh is
+// -inf, so hp = hm = -inf and the proof holds without a test of a.
 __device__ __forceinline__ float exact_skip(float a, float bh, float bl, bool& ok) {
+    const float ac = fmaxf(a, -FLT_MAX);
     const float s = __fadd_rn(a, bh);
-    const float e = __fsub_rn(bh, __fsub_rn(s, a));
+    const float sc = __fadd_rn(ac, bh);
+    const float e = __fsub_rn(bh, __fsub_rn(sc, ac));
     const float t = __fadd_rn(e, bl);
-    const float eb = __fmul_rn(__fadd_rn(fabsf(a), fabsf(bh)), kErrScale);
+    const float eb = __fmul_rn(__fadd_rn(fabsf(ac), fabsf(bh)), kErrScale);
     const float hp = __fadd_rn(s, __fadd_rn(t, eb));
     const float hm = __fadd_rn(s, __fsub_rn(t, eb));
-    const bool a_inf = a == -INFINITY;
-    ok = ((hp == hm) && (fabsf(a) >= fabsf(bh))) || a_inf;
-    return a_inf ? -INFINITY : hp;
+    ok = (hp == hm) && (fabsf(a) >= fabsf(bh));
+    return hp;
 }
 
 // max(best_du, l) with L winning ties (GPU/align_cuda.cl:536-542); all three
@@ -200,17 +206,22 @@ __device__ __forceinline__ EmSplit em_split(float em, float bh, float bl) {
 }
 
 // Score-side half: RN32(RN64(RN64(a + B) + em)) from a and the emission split;
-// a = -inf gives -inf.  `mag` = |em| + |bh|.  ok = false when not proven.
-__device__ __forceinline__ float exact_from_split(float a, EmSplit sp, float mag, bool em_finite, bool& ok) {
+// a = -inf gives -inf.  `mag` = |em| + |bh|: NaN or +inf (a division that was not
+// proven, or an infinite emission) make the candidate unproven whatever a is.
+// ok = false when not proven.  As in exact_skip, the error terms come from
+// ac = max(a, -FLT_MAX): for a = -inf, s = -inf gives hp = hm = -inf when mag
+// is finite, and NaN (not proven) when it is not.
+__device__ __forceinline__ float exact_from_split(float a, EmSplit sp, float mag, bool& ok) {
+    const float ac = fmaxf(a, -FLT_MAX);
     const float s = __fadd_rn(a, sp.p);
-    const float e = __fsub_rn(sp.p, __fsub_rn(s, a));
+    const float sc = __fadd_rn(ac, sp.p);
+    const float e = __fsub_rn(sp.p, __fsub_rn(sc, ac));
     const float t = __fadd_rn(e, sp.w);
-    const float eb = __fmul_rn(__fadd_rn(fabsf(a), mag), kErrScale);
+    const float eb = __fmul_rn(__fadd_rn(fabsf(ac), mag), kErrScale);
     const float hp = __fadd_rn(s, __fadd_rn(t, eb));
     const float hm = __fadd_rn(s, __fsub_rn(t, eb));
-    const bool a_inf = a == -INFINITY;
-    ok = ((hp == hm) && (fabsf(a) >= fabsf(sp.p))) || (a_inf && em_finite);
-    return a_inf ? -INFINITY : hp;
+    ok = (hp == hm) && (fabsf(a) >= fabsf(sp.p));
+    return hp;
 }
 
 // The next band's emission of a slot and the split for its up candidate; the
@@ -226,9 +237,8 @@ __device__ __forceinline__ NextCell next_cell(float diag, float x, float gm, flo
     NextCell n;
     bool div_ok, okd;
     n.em = emission_fast(x, gm, sd, rsd, k1, div_ok);
-    const bool fin = fabsf(n.em) < INFINITY;
     const EmSplit sd_ = em_split(n.em, c.step_h, c.step_l);
-    n.d = exact_from_split(diag, sd_, __fadd_rn(fabsf(n.em), fabsf(c.step_h)), fin, okd);
+    n.d = exact_from_split(diag, sd_, __fadd_rn(fabsf(n.em), fabsf(c.step_h)), okd);
     n.su = em_split(n.em, c.stay_h, c.stay_l);
     n.ok = div_ok && okd;
     return n;
@@ -236,7 +246,7 @@ __device__ __forceinline__ NextCell next_cell(float diag, float x, float gm, flo
 
 // The up candidate from the previous band's score of the same slot.
 __device__ __forceinline__ float cell_u(float up, const NextCell& n, const CellConsts& c, bool& ok) {
-    return exact_from_split(up, n.su, __fadd_rn(fabsf(n.em), fabsf(c.stay_h)), fabsf(n.em) < INFINITY, ok);
+    return exact_from_split(up, n.su, __fadd_rn(fabsf(n.em), fabsf(c.stay_h)), ok);
 }
 
 // max(d, u) with U winning ties (no L candidate).

@@ -39,6 +39,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "abea_cell.cuh"
 #include "abea_internal.h"
@@ -571,7 +572,7 @@ struct alignas(16) WideSmem {
     float2 emm[kWideRing][kWideChunk][kSlots];
     float sc[2][kSlots];                  // band scores, buffer b & 1
     float trim[kWideRing][kWideChunk];    // the trim cell's value of each band (-inf: past the read's events)
-    int32_t k0h[64];                      // placement of band b at [b & 63], for E
+    int32_t k0h[64];                      // placement of band b at [b & 63] (b a multiple of 4), for E
 };
 
 __device__ __forceinline__ void named_bar_sync(int id, int n) {
@@ -688,19 +689,27 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
         scores[t] = (t == 127) ? 0.0f : -INFINITY;
         scores[kSlots + t] = s1;
     }
-    int my_k0 = k0;                                      // band origins: band b in lane b & 31
+    int my_k0 = k0;                                      // band origins: band b in lane b & 31 (bands 0, 1: -51)
     uint32_t tw = 0u;                                    // backpointers of bands 4m..4m+3, byte b & 3
     uint32_t from_p = (t == 127) ? ABEA_FROM_U : 0u;     // band b-1's backpointer (band 1: the trim cell)
     int k0p = k0, e0p = e0, lop = 0, hip = 0;            // band b-1's placement and computed offsets
     unsigned long long slow = 0;
-    // band bk's bookkeeping; q1 = bk & 3 when known at compile time, else -1
+    // Band bk's bookkeeping; q1 = bk & 3 when known at compile time, else -1.  No
+    // branches: a branch in the unrolled band body splits the code the compiler
+    // schedules as one block (measured: a band-uniform branch around the
+    // last-column store cost 27 cycles per band).  The placement of every fourth
+    // band (the one E reads) goes to the ring k0h; band origins are kept one per
+    // lane of warp 0 and stored 32 bands at a time.
     auto book = [&](int bk, int q1) {
         const int qq = q1 >= 0 ? q1 : (bk & 3);
         tw |= from_p << (8 * qq);
         my_k0 = ((bk & 31) == lane) ? k0p : my_k0;
-        const int ol = n_kmers - 1 - k0p;  // last k-mer column (GPU/align_cuda.cl:722-746)
-        if (t == sl_last && ol >= lop && ol < hip && in_bounds(e0p - ol, n_events, a.counters))
-            lastc[e0p - ol] = s1;
+        if (t == 0 && (bk & 3) == 0) ws.k0h[bk & 63] = k0p;
+        {
+            const int ol = n_kmers - 1 - k0p;
+            if (t == sl_last && ol >= lop && ol < hip && in_bounds(e0p - ol, n_events, a.counters))
+                lastc[e0p - ol] = s1;
+        }
         if (kScores && in_bounds(bk, n_bands, a.counters)) scores[(int64_t)bk * kSlots + t] = s1;
     };
     auto store_tile = [&](int bk) {
@@ -708,16 +717,19 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
             reinterpret_cast<uint32_t*>(trace + (int64_t)(bk >> 2) * 512)[t] = tw;
         tw = 0u;
     };
-    auto store_origins = [&](int bk) {  // bands (bk & ~31) .. bk
-        if (warp == 0 && lane <= (bk & 31) && in_bounds((bk & ~31) + lane, n_bands, a.counters))
-            bk0[(bk & ~31) + lane] = my_k0;
+    auto store_origins = [&](int bk, bool now) {  // bands (bk & ~31) .. bk, when `now`
+        const int band = (bk & ~31) + lane;
+        if (now && warp == 0 && lane <= (bk & 31) && in_bounds(band, n_bands, a.counters)) bk0[band] = my_k0;
     };
-    for (int j = 0; j < n_chunks; ++j) {
+    // One chunk of kWideChunk bands; kLast: the read may end inside it (the only
+    // chunk that tests for the end: a test per band is a branch in the band body).
+    auto chunk = [&](int j, auto last) {
+        constexpr bool kLast = decltype(last)::value;
         const int s = j & (kWideRing - 1), bb = 2 + kWideChunk * j;
 #pragma unroll
         for (int q = 0; q < kWideChunk; ++q) {
             const int b = bb + q;
-            if (b >= n_bands) break;
+            if (kLast && b >= n_bands) break;
             named_bar_sync(kBarChain, kSlots);                   // band b-1's scores are in shared memory
             if (q == 0) named_bar_sync(kBarFull + s, kPair);     // chunk j's emissions are in the ring
             const int pb = (b - 1) & 1;
@@ -729,15 +741,14 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
             const float tv = ws.trim[s][q];
             // band b-1's bookkeeping (bands 2 + 4j + q - 1: b-1 & 3 == (q + 1) & 3)
             book(b - 1, (q + 1) & 3);
-            if (q == 2) {  // band b-1 closes a tile of four bands
+            if (q == 2) {  // band b-1 closes a tile of four bands, every eighth one 32 bands
                 store_tile(b - 1);
-                if (((b - 1) & 31) == 31) store_origins(b - 1);
+                store_origins(b - 1, ((b - 1) & 31) == 31);
             }
-            if (q == 3 && t == 0) ws.k0h[(b - 1) & 63] = k0p;  // the placement E reads for chunk j + kWideRing
             // the exact diagonal and up candidates of band b
             bool okd, oku;
-            const float d = exact_from_split(lp, EmSplit{ep.x, ep.z}, mm.x, mm.x < INFINITY, okd);
-            const float u = exact_from_split(s1, EmSplit{ep.y, ep.w}, mm.y, mm.y < INFINITY, oku);
+            const float d = exact_from_split(lp, EmSplit{ep.x, ep.z}, mm.x, okd);
+            const float u = exact_from_split(s1, EmSplit{ep.y, ep.w}, mm.y, oku);
             const bool right = band_moves_right(ll, ur, b);
             k0 += right ? 1 : 0;
             e0 += right ? 0 : 1;
@@ -764,7 +775,6 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
             }
             best = valid ? best : -INFINITY;
             from = valid ? from : 0u;
-            // the trim cell (k = -1, slot 127) while the band reaches below k-mer 0
             const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
             best = here ? tv : best;
             from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
@@ -779,12 +789,15 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
             lop = lo;
             hip = hi;
         }
-    }
+    };
+    const int n_full = (n_bands - 2) / kWideChunk;
+    for (int j = 0; j < n_full; ++j) chunk(j, std::false_type{});
+    if (n_full < n_chunks) chunk(n_full, std::true_type{});
     if (n_bands > 2) {  // the last band's bookkeeping and the stores it closes
         const int bl = n_bands - 1;
         book(bl, -1);
         store_tile(bl);
-        store_origins(bl);
+        store_origins(bl, true);
     }
     if (slow) atomicAdd(&a.counters[0], slow);
 }
@@ -1041,7 +1054,7 @@ __device__ void fill_wide_cl(const CoreArgs& a, const ReadDesc& r, ClSmem& ws, C
                     const EmSplit su{eu.x, eu.y};
                     const float mu = eu.z;
                     bool oku;
-                    const float u = exact_from_split(s_prev, su, mu, mu < INFINITY, oku);
+                    const float u = exact_from_split(s_prev, su, mu, oku);
                     const bool right = band_moves_right(ll, ur, b);
                     k0 += right ? 1 : 0;
                     e0 += right ? 0 : 1;
@@ -1084,8 +1097,7 @@ __device__ void fill_wide_cl(const CoreArgs& a, const ReadDesc& r, ClSmem& ws, C
                 const float2 ed = ws.emd[es][t];
                 const EmSplit s1{ed.x, ed.y};
                 bool okd;
-                const float d = exact_from_split(diag, s1, __fadd_rn(fabsf(em), fabsf(cc.step_h)),
-                                                 fabsf(em) < INFINITY, okd);
+                const float d = exact_from_split(diag, s1, __fadd_rn(fabsf(em), fabsf(cc.step_h)), okd);
                 const int o = (t - k0) & 127;
                 const int kk = k0 + o;
                 const int e = bn - 2 - kk;

@@ -98,6 +98,16 @@ __global__ void selftest_kernel(uint64_t seed, int iters, unsigned long long* co
             if (ok && __float_as_int(vs) != __float_as_int(rs)) ++c2;
             if (!ok) ++c3;
         }
+        // ---- a = -inf (a cell outside the band): -inf and proven for a finite
+        // emission; not proven when the emission's division was not (mag = NaN)
+        {
+            bool o1, o2, o3;
+            const float v1 = exact_skip(-INFINITY, bh, bl, o1);
+            const EmSplit sp = em_split(c, bh, bl);
+            const float v2 = exact_from_split(-INFINITY, sp, __fadd_rn(fabsf(c), fabsf(bh)), o2);
+            exact_from_split(-INFINITY, sp, __int_as_float(0x7fc00000), o3);
+            if (!o1 || v1 != -INFINITY || !o2 || v2 != -INFINITY || o3) ++c2;
+        }
     }
     atomicAdd(&counters[0], c0);
     atomicAdd(&counters[1], c1);
