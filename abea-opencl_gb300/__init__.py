@@ -31,7 +31,7 @@ LIB_PATH = os.path.join(HERE, "libabea.so")
 MODE_PLAIN = 0
 MODE_BATCHED = 1
 (OPT_MODE, OPT_STORE_SCORES, OPT_USE_GRAPH, OPT_LONG_READ_BANDS, OPT_SPIN_LIMIT, OPT_VAR_AWARE,
- OPT_TRACE_BUDGET, OPT_WIDE_CLUSTER) = range(8)
+ OPT_TRACE_BUDGET, OPT_WIDE_CLUSTER, OPT_MEDIUM_READ_BANDS) = range(9)
 
 STATUS = {
     0: "ok", -1: "invalid argument", -2: "capacity", -3: "out of memory", -4: "CUDA error",

@@ -93,6 +93,7 @@ struct abea_batch {
     std::vector<int32_t> dev_order;       // the batched form's order: wide reads, then the rest longest first
     std::vector<int32_t> dev_order_sent;  // the order last copied to the device
     int32_t n_wide = 0;          // leading reads of `order` run on the wide shape
+    int32_t n_mid = 0;           // the reads after them run on the medium shape
     // sizes
     int64_t seq_bytes = 0, n_events_total = 0, ev_pad_total = 0, km_pad_total = 0,
             band_pad_total = 0, pair_cap = 0, band_cells = 0;
@@ -142,6 +143,7 @@ struct abea_ctx {
     int64_t store_scores = 0;
     int64_t use_graph = 1;
     int64_t long_read_bands = 0;
+    int64_t mid_read_bands = 0;  // medium-shape threshold (0 = the autotuned value, else none)
     int64_t spin_limit = 1 << 22;
     int64_t var_aware = 0;
     int64_t trace_budget = 0;  // bytes of trace a read may keep (0 = every trace)
@@ -158,7 +160,8 @@ struct abea_ctx {
     abea_batch* sslot[2] = {nullptr, nullptr};
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t sev[2][4] = {};  // per slot: uploaded, compute start, compute end, results copied
-    std::map<uint64_t, int64_t> tuned;  // autotuned wide-shape threshold per workload signature
+    std::map<uint64_t, int64_t> tuned;      // autotuned wide-shape threshold per workload signature
+    std::map<uint64_t, int64_t> tuned_mid;  // autotuned medium-shape threshold per workload signature
 };
 
 // ---------------------------------------------------------------- context
@@ -253,6 +256,10 @@ extern "C" abea_status_t abea_ctx_set_option(abea_ctx_t* c, abea_option_t opt, i
         c->trace_budget = v;
         return ABEA_OK;
     case ABEA_OPT_WIDE_CLUSTER: c->wide_cluster = v != 0; return ABEA_OK;
+    case ABEA_OPT_MEDIUM_READ_BANDS:
+        if (v < 0) return fail(ABEA_ERR_INVALID_ARG, "negative band threshold");
+        c->mid_read_bands = v;
+        return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -268,6 +275,7 @@ extern "C" abea_status_t abea_ctx_get_option(abea_ctx_t* c, abea_option_t opt, i
     case ABEA_OPT_VAR_AWARE: *v = c->var_aware; return ABEA_OK;
     case ABEA_OPT_TRACE_BUDGET: *v = c->trace_budget; return ABEA_OK;
     case ABEA_OPT_WIDE_CLUSTER: *v = c->wide_cluster; return ABEA_OK;
+    case ABEA_OPT_MEDIUM_READ_BANDS: *v = c->mid_read_bands; return ABEA_OK;
     }
     return fail(ABEA_ERR_INVALID_ARG, "unknown option %d", (int)opt);
 }
@@ -607,24 +615,32 @@ static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
     return best_n > 0 ? wide_ok[(size_t)best_n - 1] : INT64_MAX;
 }
 
-// Reads of the batched form that run on the wide shape: the longest reads over
-// the threshold (the option, the autotuned value, or the heuristic above), at most
-// one per resident block, never a checkpointed read.  Fills b->dev_order with
-// those reads first, then the rest longest first.
-static int choose_wide_reads(abea_batch* b, int sm_count, int64_t threshold, bool scores, bool cluster) {
+// Reads of the batched form that run on the wide and the medium shapes: the
+// longest reads over the wide threshold (the option, the autotuned value, or the
+// heuristic above), at most one per resident block, then the longest remaining
+// reads over the medium threshold (none without one; never with the cluster
+// pair); never a checkpointed read.  Fills b->dev_order with the wide reads, the
+// medium reads, then the rest, each longest first, and sets n_wide and n_mid.
+static void choose_shape_reads(abea_batch* b, int sm_count, int64_t threshold, int64_t mid_threshold, bool scores,
+                               bool cluster) {
     const int blocks = cluster ? sm_count / 2 : batched_blocks_per_sm(scores) * sm_count;
     if (threshold <= 0) threshold = heuristic_threshold(b, blocks);
-    std::vector<int32_t> wide, rest;
+    if (mid_threshold <= 0 || cluster) mid_threshold = INT64_MAX;
+    std::vector<int32_t> wide, mid, rest;
     for (int32_t i : b->order) {
         const ReadDesc& r = b->reads[(size_t)i];
         if ((int)wide.size() < blocks && !r.ck && r.n_bands >= threshold)
             wide.push_back(i);
+        else if (!r.ck && r.n_bands >= mid_threshold)
+            mid.push_back(i);
         else
             rest.push_back(i);
     }
     b->dev_order = wide;
+    b->dev_order.insert(b->dev_order.end(), mid.begin(), mid.end());
     b->dev_order.insert(b->dev_order.end(), rest.begin(), rest.end());
-    return (int)wide.size();
+    b->n_wide = (int32_t)wide.size();
+    b->n_mid = (int32_t)mid.size();
 }
 
 // Queues pre, core and post for a batch on the context's stream.
@@ -637,7 +653,7 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
                        b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
                        b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch, b->d_spec,
                        b->n_spec,
-                       (long long)c->spin_limit};
+                       (long long)c->spin_limit, b->n_mid};
     la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1, b->d_km_rsd,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
                        b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event};
@@ -673,16 +689,23 @@ static abea_status_t queue_work(abea_ctx* c, abea_batch* b, int* launches, bool 
 }
 
 // The batched form's order: wide reads (threshold from the option, else the
-// autotuned value of this workload signature, else the heuristic) then the rest.
+// autotuned value of this workload signature, else the heuristic), medium reads
+// (threshold from the option, else the autotuned value, else none), then the rest.
 static void prepare_order(abea_ctx* c, abea_batch* b) {
     b->n_wide = 0;
+    b->n_mid = 0;
     if (c->mode != ABEA_MODE_BATCHED) return;
-    int64_t thr = c->long_read_bands;
+    const uint64_t sig = workload_signature(b);
+    int64_t thr = c->long_read_bands, mid = c->mid_read_bands;
     if (thr == 0) {
-        auto it = c->tuned.find(workload_signature(b));
+        auto it = c->tuned.find(sig);
         if (it != c->tuned.end()) thr = it->second;
     }
-    b->n_wide = choose_wide_reads(b, c->sm_count, thr, b->scores_kept, c->wide_cluster != 0);
+    if (mid == 0) {
+        auto it = c->tuned_mid.find(sig);
+        if (it != c->tuned_mid.end()) mid = it->second;
+    }
+    choose_shape_reads(b, c->sm_count, thr, mid, b->scores_kept, c->wide_cluster != 0);
 }
 
 static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
@@ -711,6 +734,7 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
         std::vector<uint64_t> key = b->carve;
         key.push_back((uint64_t)b->n_reads);
         key.push_back((uint64_t)b->n_wide);
+        key.push_back((uint64_t)b->n_mid);
         key.push_back((uint64_t)(b->scores_kept ? 1 : 0) | ((uint64_t)b->var_aware << 1) |
                       ((uint64_t)(c->wide_cluster != 0) << 2));
         if (!b->graph || key != b->graph_key) {
@@ -792,23 +816,75 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
             best = cand;
         }
     }
+    // then the medium shape with that wide threshold: none, or the band count of
+    // the reads that leave k of the remaining reads for it (k from a quarter of the
+    // block halves to four per half) or at fractions of the longest remaining read
+    const int64_t mid0 = c->mid_read_bands;
+    int64_t best_mid = INT64_MAX;
+    if (!st && c->wide_cluster == 0) {
+        c->long_read_bands = best;
+        std::vector<int64_t> rest;  // band counts of the reads left after the wide ones, longest first
+        int n_wide_best = 0;
+        for (int32_t i : b->order) {
+            const ReadDesc& r = b->reads[(size_t)i];
+            if (n_wide_best < blocks && !r.ck && r.n_bands >= best) {
+                ++n_wide_best;
+                continue;
+            }
+            if (!r.ck) rest.push_back(r.n_bands);
+        }
+        std::vector<int64_t> mids;
+        for (int num : {1, 2, 4, 8, 16}) {  // num/2 medium reads per block half
+            const size_t k = (size_t)std::max(1, blocks * 2 * num / 4);
+            if (k <= rest.size()) {
+                const int64_t v = std::max<int64_t>(1, rest[k - 1]);
+                if (std::find(mids.begin(), mids.end(), v) == mids.end()) mids.push_back(v);
+            }
+        }
+        if (!rest.empty())
+            for (int pct : {25, 50, 75}) {
+                const int64_t v = std::max<int64_t>(1, rest[0] * pct / 100);
+                if (std::find(mids.begin(), mids.end(), v) == mids.end()) mids.push_back(v);
+            }
+        for (int64_t cand : mids) {
+            c->mid_read_bands = cand;
+            float t_min = 1e30f;
+            for (int rep = 0; rep < 3 && !st; ++rep) {
+                if ((st = run_batch(c, b))) break;
+                if ((st = collect_timing(c, b))) break;
+                if (rep > 0) t_min = std::min(t_min, b->timing.total_ms);
+            }
+            if (st) break;
+            if (t_min < best_t * 0.98f) {  // the medium shape must buy 2%
+                best_t = t_min;
+                best_mid = cand;
+            }
+        }
+    }
     c->mode = mode0;
     c->long_read_bands = thr0;
+    c->mid_read_bands = mid0;
     if (st) return st;
     c->tuned[workload_signature(b)] = best;
+    c->tuned_mid[workload_signature(b)] = best_mid;
     if (best_threshold) *best_threshold = best;
     if (best_ms) *best_ms = best_t;
     return ABEA_OK;
 }
 
-// Autotuner cache: "abea-autotune 1 sm_count <n>" then "<signature> <threshold>" lines.
+// Autotuner cache: "abea-autotune 2 sm_count <n>" then "<signature> <wide threshold>
+// <medium threshold>" lines (INT64_MAX = none).  Version 1 files (no medium
+// threshold) are read too.
 extern "C" abea_status_t abea_autotune_save(abea_ctx_t* c, const char* path, int32_t* n_entries) {
     if (!c || !path) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_save: null argument");
     FILE* f = fopen(path, "w");
     if (!f) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_save: cannot open %s", path);
-    fprintf(f, "abea-autotune 1 sm_count %d\n", c->sm_count);
-    for (const auto& kv : c->tuned)
-        fprintf(f, "%llu %lld\n", (unsigned long long)kv.first, (long long)kv.second);
+    fprintf(f, "abea-autotune 2 sm_count %d\n", c->sm_count);
+    for (const auto& kv : c->tuned) {
+        auto m = c->tuned_mid.find(kv.first);
+        fprintf(f, "%llu %lld %lld\n", (unsigned long long)kv.first, (long long)kv.second,
+                (long long)(m == c->tuned_mid.end() ? INT64_MAX : m->second));
+    }
     const bool ok = fclose(f) == 0;
     if (!ok) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_save: write to %s failed", path);
     if (n_entries) *n_entries = (int32_t)c->tuned.size();
@@ -820,7 +896,7 @@ extern "C" abea_status_t abea_autotune_load(abea_ctx_t* c, const char* path, int
     FILE* f = fopen(path, "r");
     if (!f) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: cannot open %s", path);
     int version = 0, sm = 0;
-    if (fscanf(f, "abea-autotune %d sm_count %d", &version, &sm) != 2 || version != 1) {
+    if (fscanf(f, "abea-autotune %d sm_count %d", &version, &sm) != 2 || (version != 1 && version != 2)) {
         fclose(f);
         return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: %s is not an autotuner cache", path);
     }
@@ -829,21 +905,26 @@ extern "C" abea_status_t abea_autotune_load(abea_ctx_t* c, const char* path, int
         return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: %s was tuned on %d SMs, this device has %d", path,
                     sm, c->sm_count);
     }
-    std::map<uint64_t, int64_t> got;
+    std::map<uint64_t, std::pair<int64_t, int64_t>> got;
     unsigned long long sig = 0;
-    long long thr = 0;
+    long long thr = 0, mid = INT64_MAX;
+    const int fields = version == 1 ? 2 : 3;
     int r;
-    while ((r = fscanf(f, "%llu %lld", &sig, &thr)) == 2) {
-        if (thr < 1) {
+    while ((r = version == 1 ? fscanf(f, "%llu %lld", &sig, &thr) : fscanf(f, "%llu %lld %lld", &sig, &thr, &mid)) ==
+           fields) {
+        if (thr < 1 || mid < 1) {
             fclose(f);
             return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: bad threshold in %s", path);
         }
-        got[(uint64_t)sig] = (int64_t)thr;
+        got[(uint64_t)sig] = {(int64_t)thr, (int64_t)mid};
     }
     const bool at_end = r == EOF;
     fclose(f);
     if (!at_end) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune_load: malformed line in %s", path);
-    for (const auto& kv : got) c->tuned[kv.first] = kv.second;
+    for (const auto& kv : got) {
+        c->tuned[kv.first] = kv.second.first;
+        c->tuned_mid[kv.first] = kv.second.second;
+    }
     if (n_entries) *n_entries = (int32_t)got.size();
     return ABEA_OK;
 }

@@ -554,26 +554,36 @@ __device__ void fill_warp(const CoreArgs& a, const ReadDesc& r, Rings& rg, int l
 // bands before the chunk's last band.  B and E hand the ring slots over with
 // named barriers, FULL[s] (E arrives, B waits) and EMPTY[s] (B arrives, E waits);
 // every use of a barrier completes before its next, so arrivals never pile up.
+//
+// The medium shape is the same chain and producer with one E group (warps 4-7)
+// and a ring of kMidRing chunks: eight warps per read, two reads per block (warps
+// 0-7 and 8-15), each half on its own named barriers.
 constexpr int kWideThreads = 512;   // block size of the batched kernel
 constexpr int kWideChunk = 4;       // bands per emission chunk
-constexpr int kWideRing = 4;        // chunks in the ring (kWideChunk * kWideRing + 1 <= 28)
-constexpr int kBarChain = 1;        // B's per-band barrier
-constexpr int kBarFull = 2;         // FULL[s] = kBarFull + s
-constexpr int kBarEmpty = kBarFull + kWideRing;  // EMPTY[s] = kBarEmpty + s
+constexpr int kWideRing = 4;        // chunks in the wide shape's ring (kWideChunk * ring + 1 <= 28)
+constexpr int kMidRing = 2;         // chunks in the medium shape's ring
+constexpr int kMidThreads = 256;    // threads per medium read
+// Named barriers of one read (IDs from a base): base = B's per-band barrier,
+// base + 1 + s = FULL[s], base + 1 + ring + s = EMPTY[s]; the medium shape adds
+// base + 1 + 2 * ring, the half-block barrier between its reads.
+constexpr int kMidBars = 2 + 2 * kMidRing;
 static_assert(kWideChunk * kWideRing + 1 <= 28, "E's k-mer window must hold the chunk's bands");
 static_assert(kWideRing % 2 == 0, "each ring slot, and its two barriers, belongs to one of the two E groups");
-static_assert(kBarEmpty + kWideRing <= 16, "named barriers 0-15");
+static_assert(1 + 1 + 2 * kWideRing <= 16 && 1 + 2 * kMidBars <= 16, "named barriers 0-15");
 
-struct alignas(16) WideSmem {
-    // band kWideChunk*j + 2 + q of chunk j in slot j % kWideRing, entry [q]:
+template <int kRing>
+struct alignas(16) ChainSmem {
+    // band kWideChunk*j + 2 + q of chunk j in slot j % kRing, entry [q]:
     // {p_step, p_stay, w_step, w_stay} and {|em| + |step_h|, |em| + |stay_h|} (NaN
     // when the emission's division was not proven)
-    float4 ems[kWideRing][kWideChunk][kSlots];
-    float2 emm[kWideRing][kWideChunk][kSlots];
+    float4 ems[kRing][kWideChunk][kSlots];
+    float2 emm[kRing][kWideChunk][kSlots];
     float sc[2][kSlots];                  // band scores, buffer b & 1
-    float trim[kWideRing][kWideChunk];    // the trim cell's value of each band (-inf: past the read's events)
+    float trim[kRing][kWideChunk];        // the trim cell's value of each band (-inf: past the read's events)
     int32_t k0h[64];                      // placement of band b at [b & 63] (b a multiple of 4), for E
 };
+using WideSmem = ChainSmem<kWideRing>;
+using MidSmem = ChainSmem<kMidRing>;
 
 __device__ __forceinline__ void named_bar_sync(int id, int n) {
     asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(n) : "memory");
@@ -588,9 +598,10 @@ __device__ __forceinline__ bool band_moves_right(float ll, float ur, int b) {
 }
 
 // E: chunk j's emissions for slot t, from the placement kp of an earlier band.
-__device__ __forceinline__ void wide_chunk(WideSmem& ws, const CoreArgs& a, const ReadDesc& r, const CellConsts& cc,
-                                           int t, int j, int kp) {
-    const int s = j & (kWideRing - 1), bb = 2 + kWideChunk * j;
+template <int kRing>
+__device__ __forceinline__ void wide_chunk(ChainSmem<kRing>& ws, const CoreArgs& a, const ReadDesc& r,
+                                           const CellConsts& cc, int t, int j, int kp) {
+    const int s = j % kRing, bb = 2 + kWideChunk * j;
     const int kk = kp + ((t - kp) & (kSlots - 1));  // slot t's k-mer in the window
     const bool kin = kk >= 0 && kk < r.n_kmers;
     const int64_t ko = r.km_off + (kin ? kk : 0);
@@ -640,27 +651,32 @@ __device__ __noinline__ SlowCell slow_cell_call(float diag, float up, float left
     return o;
 }
 
-// Called by all kWideThreads threads of a block; warps 12 and up return at once.
-template <bool kScores>
-__device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, int tid) {
+// One read's fill by warps 0 .. 4 + 4 * kGroups - 1 of the calling threads
+// (tid = index among them; others return at once): B = warps 0-3, E = the
+// kGroups groups of four warps after them, group g taking chunks g, g + kGroups,
+// ...  bar0 = the read's first named barrier.  The wide shape is kGroups = 2 with
+// kWideRing chunks, the medium shape kGroups = 1 with kMidRing.
+template <bool kScores, int kGroups, int kRing>
+__device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing>& ws, int tid, int bar0) {
+    static_assert(kGroups == 1 || kRing % kGroups == 0, "each ring slot belongs to one E group");
     const int warp = tid >> 5;
-    if (warp >= 12) return;
+    if (warp >= 4 + 4 * kGroups) return;
     const CellConsts cc = make_consts(r, a.g);
     const int n_events = r.n_events, n_kmers = r.n_kmers, n_bands = r.n_bands;
     const int n_chunks = (n_bands - 2 + kWideChunk - 1) / kWideChunk;
     const int t = tid & (kSlots - 1);
     constexpr int kPair = 2 * kSlots;  // B and E threads on FULL / EMPTY
+    const int kBarChain = bar0, kBarFull = bar0 + 1, kBarEmpty = bar0 + 1 + kRing;
 
     if (warp >= 4) {
-        // ------------------------------------------------ E: the emission chunks,
-        // E0 (warps 4-7) the even ones, E1 (warps 8-11) the odd ones: each group has
-        // two chunks of B's time for the loads and arithmetic of one
-        for (int j = (warp >> 2) - 1; j < n_chunks; j += 2) {
-            const int s = j & (kWideRing - 1);
-            int kp = -1 - kBand / 2;  // band 1's placement, for the first kWideRing chunks
-            if (j >= kWideRing) {
-                named_bar_sync(kBarEmpty + s, kPair);  // B released chunk j - kWideRing
-                kp = ws.k0h[(kWideChunk * (j - kWideRing) + kWideChunk) & 63];  // band bb(j - R) + C - 2
+        // ------------------------------------------------ E: the emission chunks; with
+        // two groups each has two chunks of B's time for the loads and arithmetic of one
+        for (int j = (warp >> 2) - 1; j < n_chunks; j += kGroups) {
+            const int s = j % kRing;
+            int kp = -1 - kBand / 2;  // band 1's placement, for the first kRing chunks
+            if (j >= kRing) {
+                named_bar_sync(kBarEmpty + s, kPair);  // B released chunk j - kRing
+                kp = ws.k0h[(kWideChunk * (j - kRing) + kWideChunk) & 63];  // band bb(j - R) + C - 2
             }
             wide_chunk(ws, a, r, cc, t, j, kp);
             named_bar_arrive(kBarFull + s, kPair);
@@ -725,7 +741,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
     // chunk that tests for the end: a test per band is a branch in the band body).
     auto chunk = [&](int j, auto last) {
         constexpr bool kLast = decltype(last)::value;
-        const int s = j & (kWideRing - 1), bb = 2 + kWideChunk * j;
+        const int s = j % kRing, bb = 2 + kWideChunk * j;
 #pragma unroll
         for (int q = 0; q < kWideChunk; ++q) {
             const int b = bb + q;
@@ -779,7 +795,7 @@ __device__ void fill_wide(const CoreArgs& a, const ReadDesc& r, WideSmem& ws, in
             best = here ? tv : best;
             from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
             ws.sc[b & 1][t] = best;
-            if (q == kWideChunk - 1 && j + kWideRing < n_chunks)
+            if (q == kWideChunk - 1 && j + kRing < n_chunks)
                 named_bar_arrive(kBarEmpty + s, kPair);  // chunk j read: E may refill its slot
             lp = left;
             s1 = best;
@@ -1910,9 +1926,13 @@ constexpr int kBatchedWarps = kWideThreads / 32;
 struct BatchedSmem {
     WideSmem wide;                     // phase 1: the block's wide read
     Rings warp_rings[kBatchedWarps];   // phase 2: one per warp
-    PostSmem post[kBatchedWarps];      // every warp's post staging
+    // every warp's post staging; in phase 1b each half's medium read uses its eight
+    // warps' entries (post[8 * half] on), which no other warp touches meanwhile
+    PostSmem post[kBatchedWarps];
     int32_t pick;                      // the block's wide read, or -1
-    int32_t free_rank;                 // rank among the blocks without a wide read, or -1
+    int32_t free_rank;                 // rank among the blocks with neither a wide nor medium reads, or -1
+    int32_t mid_block;                 // 1: a block of the medium reads
+    int32_t mid_pick[2];               // each half's medium read
 };
 static_assert(offsetof(BatchedSmem, warp_rings) % 16 == 0 && offsetof(BatchedSmem, post) % 16 == 0 &&
                   sizeof(Rings) % 16 == 0 && sizeof(PostSmem) % 16 == 0,
@@ -1923,6 +1943,9 @@ static_assert(offsetof(WideSmem, ems) % 16 == 0 && offsetof(WideSmem, emm) % 8 =
 static_assert(sizeof(WideSmem) >= kPostRingDeep * kPostChunkBands * kSlots && alignof(WideSmem) >= 16,
               "the wide read's traceback ring lives in the wide fill's shared memory");
 static_assert(sizeof(WidePostSmem) <= sizeof(WideSmem), "the wide read's traceback state fits the fill's memory");
+static_assert(sizeof(MidSmem) <= (kBatchedWarps / 2) * sizeof(PostSmem) &&
+                  sizeof(MidSmem) >= kPostRingDeep * kPostChunkBands * kSlots,
+              "a medium read's fill, and then its traceback ring, fit its half's post staging");
 
 
 
@@ -1932,10 +1955,15 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
     BatchedSmem& sm = *reinterpret_cast<BatchedSmem*>(smem_raw);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     // phase 1: one of the longest reads on the wide shape
+    // The first blocks to arrive take the wide reads, one each; the next ones the
+    // medium reads (two at a time per block, enough blocks for each half to start
+    // one); the others the first wave of the warp-shape reads.
+    const int n_midb = min((a.n_mid + 1) / 2, max((int)gridDim.x - a.n_wide, 0));
     if (t == 0) {
         const int q = atomicAdd(&a.queue[0], 1);
         sm.pick = q < a.n_wide ? a.order[q] : -1;
-        sm.free_rank = q < a.n_wide ? -1 : q - a.n_wide;
+        sm.mid_block = (q >= a.n_wide && q < a.n_wide + n_midb) ? 1 : 0;
+        sm.free_rank = q < a.n_wide + n_midb ? -1 : q - a.n_wide - n_midb;
     }
     __syncthreads();
     const int wide_read = sm.pick, free_rank = sm.free_rank;
@@ -1943,18 +1971,42 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         const ReadDesc& r = a.reads[wide_read];
         pre_read(pa, wide_read, t, kWideThreads);
         __syncthreads();  // the read's parameters are in memory for the whole block
-        if (!r.skip) fill_wide<kScores>(a, r, sm.wide, t);
+        if (!r.skip) fill_chain<kScores, 2, kWideRing>(a, r, sm.wide, t, 1);
         __syncthreads();
         __threadfence_block();
         // the whole block walks the wide read's traceback (the fill's shared memory is free)
         post_wide_block(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0], t);
     }
-    // phase 2: the first wave is static, the blocks without a wide read taking the
-    // longest remaining reads round-robin (warp w of free block f: read f + F*w),
-    // so that the long ones spread over the SMs; then every warp pulls the rest
-    // longest-first
-    const int n_rest = a.n_reads - a.n_wide;
-    const int n_free = (int)gridDim.x - min(a.n_wide, (int)gridDim.x);
+    // phase 1b: the medium reads, each half of a medium block (eight warps) pulling
+    // one at a time: pre, fill, and the traceback by the half's first warp; the
+    // blocks done with a wide read join in
+    if (a.n_mid > 0 && free_rank < 0) {
+        if (wide_read >= 0) __syncthreads();  // the wide read's traceback is done with its memory
+        const int half = warp >> 3, ht = t & (kMidThreads - 1), hw = ht >> 5;
+        MidSmem& ms = *reinterpret_cast<MidSmem*>(&sm.post[half * (kBatchedWarps / 2)]);
+        const int bar0 = 1 + half * kMidBars, bar_half = bar0 + kMidBars - 1;
+        while (true) {
+            if (ht == 0) sm.mid_pick[half] = atomicAdd(&a.queue[3], 1);
+            named_bar_sync(bar_half, kMidThreads);  // the pick is visible; the last read's traceback is done
+            const int q = sm.mid_pick[half];
+            if (q >= a.n_mid) break;  // the whole half leaves together
+            const int ri = a.order[a.n_wide + q];
+            const ReadDesc& r = a.reads[ri];
+            pre_read(pa, ri, ht, kMidThreads);
+            named_bar_sync(bar_half, kMidThreads);  // the read's parameters are in memory; the pick was read
+            if (!r.skip) fill_chain<kScores, 1, kMidRing>(a, r, ms, ht, bar0);
+            named_bar_sync(bar_half, kMidThreads);  // the fill is done: its memory becomes the traceback ring
+            __threadfence_block();
+            if (hw == 0) post_read_warp<kPostRingDeep>(a, p, ri, reinterpret_cast<uint8_t*>(&ms), sm.warp_rings[warp], lane);
+        }
+    }
+    // phase 2: the first wave is static, the blocks with neither a wide nor medium
+    // reads taking the longest remaining reads round-robin (warp w of free block f:
+    // read f + F*w), so that the long ones spread over the SMs; then every warp
+    // pulls the rest longest-first.
+    const int n_pre = a.n_wide + a.n_mid;
+    const int n_rest = a.n_reads - n_pre;
+    const int n_free = max((int)gridDim.x - a.n_wide - n_midb, 0);
     const int wave = min(n_rest, n_free * kBatchedWarps);
     for (int pass = 0;; ++pass) {
         int q;
@@ -1968,7 +2020,7 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
             q = __shfl_sync(kFull, q, 0);
             if (q >= n_rest) break;
         }
-        const int ri = a.order[a.n_wide + q];
+        const int ri = a.order[n_pre + q];
         const ReadDesc& r = a.reads[ri];
         pre_read(pa, ri, lane, 32);
         __syncwarp();  // the read's parameters are in memory for the warp

@@ -48,6 +48,7 @@ struct CoreArgs {
     int32_t* spec;                 // traceback cell maps: kSpecRound * kSpecBands int32 per slot
     int32_t n_spec;                // slots (queue[2] hands them out)
     long long spin_limit;          // polls before a device-side wait gives up (counters[2] counts those)
+    int32_t n_mid;                 // the reads after the wide ones that run on the medium shape (batched form)
 };
 
 struct PostArgs {

@@ -133,9 +133,12 @@ typedef enum {
                                    needing more keeps band-score checkpoints every 256 bands (4 bytes per
                                    band) and its traceback recomputes the trace 256 bands at a time.
                                    0 (default) = keep every trace.  Taken at batch creation. */
-    ABEA_OPT_WIDE_CLUSTER = 7   /* BATCHED: 1 = the longest reads run on a cluster of two blocks (the
+    ABEA_OPT_WIDE_CLUSTER = 7,  /* BATCHED: 1 = the longest reads run on a cluster of two blocks (the
                                    second SM computes the emissions ahead into the first one's shared
                                    memory); 0 = one block per wide read */
+    ABEA_OPT_MEDIUM_READ_BANDS = 8 /* BATCHED: reads with at least this many bands that do not take the
+                                   wide shape run on the medium shape (eight warps per read, two reads
+                                   per block); 0 = autotuned (none when not tuned) */
 } abea_option_t;
 
 typedef struct abea_ctx abea_ctx_t;

@@ -69,17 +69,21 @@ def test_edge_cases_match_reference(lib, oracle_mod, ref_synthetic, mode):
         assert np.array_equal(bll.view(np.int32).reshape(-1, 2), rbll), name
 
 
-@pytest.mark.parametrize("shape", ["warp", "wide"])
+@pytest.mark.parametrize("shape", ["warp", "wide", "medium"])
 @pytest.mark.parametrize("seed", [1, 2, 4])
 def test_small_workload_bit_exact(lib, oracle_mod, seed, shape):
-    """Every score, backpointer and band origin of three reads, and every read's
-    best score, against the oracle: on the warp shape (plain form) and on the
-    wide shape (batched form with every read wide)."""
+    """Every score, backpointer and band origin of four reads, and every read's
+    best score, against the oracle: on the warp shape (plain form), on the wide
+    shape (batched form with every read wide) and on the medium shape (batched
+    form with every read medium, two per block)."""
     from abea_gb300 import synth
     batch = synth.make_batch("small", seed=seed)
     ctx = abea.Context(0, abea.MODE_PLAIN if shape == "warp" else abea.MODE_BATCHED, store_scores=True)
     if shape == "wide":
         ctx.set_option(abea.OPT_LONG_READ_BANDS, 1)
+    if shape == "medium":
+        ctx.set_option(abea.OPT_LONG_READ_BANDS, 1 << 40)
+        ctx.set_option(abea.OPT_MEDIUM_READ_BANDS, 1)
     dev = ctx.upload(batch)
     dev.run()
     gp, gc = dev.results()
@@ -226,6 +230,27 @@ def test_error_against_fp64_is_bounded(lib, oracle_mod, workload):
     assert e["reads_with_other_pairs"] <= max(3, batch.n_reads // 20)
 
 
+@pytest.mark.parametrize("wide_reads, medium_reads", [(0, 300), (8, 200), (30, 600)])
+def test_three_shapes_in_one_batch(lib, oracle_mod, wide_reads, medium_reads):
+    """The wide shape for the longest reads, the medium shape (two reads per block)
+    for the next ones, one warp per read for the rest, in one launch: AlignedPairs
+    and best scores bit-exact with the oracle, and the same through the graph
+    replay of a second run."""
+    from abea_gb300 import synth
+    batch = synth.make_batch("reads1024", seed=3)
+    nb = np.sort(batch.n_bands())[::-1]
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    ctx.set_option(abea.OPT_LONG_READ_BANDS, int(nb[wide_reads - 1]) if wide_reads else 1 << 40)
+    ctx.set_option(abea.OPT_MEDIUM_READ_BANDS, int(nb[wide_reads + medium_reads - 1]))
+    dev = ctx.upload(batch)
+    op, oc, obest = oracle_batch(oracle_mod, batch)
+    for _ in range(2):
+        dev.run()
+        gp, gc = dev.results()
+        assert_same_alignments(batch, gp, gc, op, oc)
+        assert np.array_equal(dev.best_scores().view(np.uint32), obest.view(np.uint32))
+
+
 def test_uneven_batch_batched_equals_plain(lib):
     """Heavy-tailed 1.3 Mbase batch: batched (wide + warp shapes, fused post) and
     plain forms give identical AlignedPairs."""
@@ -327,11 +352,17 @@ def test_autotuner_cache_round_trip(lib, tmp_path):
     p2, c2 = other.align_batch(batch)
     assert_same_alignments(batch, p1, c1, p2, c2)
     lines = open(path).read().split("\n")
-    assert lines[0].startswith("abea-autotune 1 sm_count ") and lines[1].split()[1] == str(thr)
+    assert lines[0].startswith("abea-autotune 2 sm_count ") and lines[1].split()[1] == str(thr)
+    assert int(lines[1].split()[2]) >= 1  # the medium threshold (INT64_MAX: none)
+    assert other.get_option(abea.OPT_MEDIUM_READ_BANDS) == 0
     (tmp_path / "bad.txt").write_text("not a cache\n")
     with pytest.raises(abea.AbeaError):
         other.autotune_load(str(tmp_path / "bad.txt"))
     sm = int(lines[0].split()[-1])
-    (tmp_path / "other_gpu.txt").write_text(f"abea-autotune 1 sm_count {sm + 1}\n{lines[1]}\n")
+    (tmp_path / "other_gpu.txt").write_text(f"abea-autotune 2 sm_count {sm + 1}\n{lines[1]}\n")
     with pytest.raises(abea.AbeaError):
         other.autotune_load(str(tmp_path / "other_gpu.txt"))
+    # a version 1 file (wide threshold only) still loads
+    sig, wide = lines[1].split()[:2]
+    (tmp_path / "v1.txt").write_text(f"abea-autotune 1 sm_count {sm}\n{sig} {wide}\n")
+    assert other.autotune_load(str(tmp_path / "v1.txt")) == 1
