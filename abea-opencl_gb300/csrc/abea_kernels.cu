@@ -716,12 +716,12 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     // last-column store cost 27 cycles per band).  The placement of every fourth
     // band (the one E reads) goes to the ring k0h; band origins are kept one per
     // lane of warp 0 and stored 32 bands at a time.
-    auto book = [&](int bk, int q1) {
+    auto book = [&](int bk, int q1, bool last_col) {
         const int qq = q1 >= 0 ? q1 : (bk & 3);
         tw |= from_p << (8 * qq);
         my_k0 = ((bk & 31) == lane) ? k0p : my_k0;
         if (t == 0 && (bk & 3) == 0) ws.k0h[bk & 63] = k0p;
-        {
+        if (last_col) {
             const int ol = n_kmers - 1 - k0p;
             if (t == sl_last && ol >= lop && ol < hip && in_bounds(e0p - ol, n_events, a.counters))
                 lastc[e0p - ol] = s1;
@@ -739,8 +739,13 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     };
     // One chunk of kWideChunk bands; kLast: the read may end inside it (the only
     // chunk that tests for the end: a test per band is a branch in the band body).
-    auto chunk = [&](int j, auto last) {
-        constexpr bool kLast = decltype(last)::value;
+    // kMid: a chunk inside the read, where every band's computed cells are all 100
+    // (offsets [0, 100)), none is the trim cell and none lies on the last k-mer
+    // column (and neither does band bb-1, whose bookkeeping the chunk finishes): k0
+    // and e0 each move by at most one per band, so the placement of band bb-1
+    // decides it for the whole chunk.
+    auto chunk = [&](int j, auto last, auto mid) {
+        constexpr bool kLast = decltype(last)::value, kMid = decltype(mid)::value;
         const int s = j % kRing, bb = 2 + kWideChunk * j;
 #pragma unroll
         for (int q = 0; q < kWideChunk; ++q) {
@@ -756,7 +761,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const float2 mm = ws.emm[s][q][t];
             const float tv = ws.trim[s][q];
             // band b-1's bookkeeping (bands 2 + 4j + q - 1: b-1 & 3 == (q + 1) & 3)
-            book(b - 1, (q + 1) & 3);
+            book(b - 1, (q + 1) & 3, !kMid);
             if (q == 2) {  // band b-1 closes a tile of four bands, every eighth one 32 bands
                 store_tile(b - 1);
                 store_origins(b - 1, ((b - 1) & 31) == 31);
@@ -768,10 +773,10 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const bool right = band_moves_right(ll, ur, b);
             k0 += right ? 1 : 0;
             e0 += right ? 0 : 1;
-            int lo, hi;
-            band_range(k0, e0, n_events, n_kmers, lo, hi);
+            int lo = 0, hi = kBand;
+            if (!kMid) band_range(k0, e0, n_events, n_kmers, lo, hi);
             const int o = (t - k0) & 127;
-            const bool valid = o >= lo && o < hi;
+            const bool valid = kMid ? o < kBand : (o >= lo && o < hi);
             // d vs u (U wins ties), then the skip candidate (L wins ties)
             uint32_t from_du, from;
             const float best_du = pick_du(d, u, from_du);
@@ -791,9 +796,11 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             }
             best = valid ? best : -INFINITY;
             from = valid ? from : 0u;
-            const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
-            best = here ? tv : best;
-            from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
+            if (!kMid) {
+                const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
+                best = here ? tv : best;
+                from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
+            }
             ws.sc[b & 1][t] = best;
             if (q == kWideChunk - 1 && j + kRing < n_chunks)
                 named_bar_arrive(kBarEmpty + s, kPair);  // chunk j read: E may refill its slot
@@ -807,11 +814,16 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
         }
     };
     const int n_full = (n_bands - 2) / kWideChunk;
-    for (int j = 0; j < n_full; ++j) chunk(j, std::false_type{});
-    if (n_full < n_chunks) chunk(n_full, std::true_type{});
+    for (int j = 0; j < n_full; ++j) {
+        if (k0 >= 0 && k0 + kWideChunk <= n_kmers - 1 - kBand && e0 >= kBand - 1 && e0 + kWideChunk <= n_events - 1)
+            chunk(j, std::false_type{}, std::true_type{});
+        else
+            chunk(j, std::false_type{}, std::false_type{});
+    }
+    if (n_full < n_chunks) chunk(n_full, std::true_type{}, std::false_type{});
     if (n_bands > 2) {  // the last band's bookkeeping and the stores it closes
         const int bl = n_bands - 1;
-        book(bl, -1);
+        book(bl, -1, true);
         store_tile(bl);
         store_origins(bl, true);
     }
