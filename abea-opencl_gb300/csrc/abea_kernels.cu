@@ -784,15 +784,18 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const float l = exact_skip(left, cc.skip_h, cc.skip_l, okl);
             float best = pick_l(best_du, from_du, l, from);
             const bool bad = valid && !(okd && oku && okl);
-            if (__any_sync(kFull, bad)) {  // warp-uniform and rare
-                if (bad) {  // a proof failed: the reference's FP64 arithmetic
-                    const int64_t ko = r.km_off + (k0 + o);
-                    const SlowCell c = slow_cell_call(lp, s1, left, a.ev_mean[r.ev_off + (e0 - o)], a.km_gm[ko],
-                                                      a.km_sd[ko], a.km_k1[ko], cc.lp_step, cc.lp_stay, cc.lp_skip);
-                    best = c.best;
-                    from = c.from;
-                    ++slow;
-                }
+            if (__any_sync(kFull, bad)) {
+                // Rare: a proof failed in some lane, whose cell takes the reference's
+                // FP64 arithmetic.  The whole warp calls (a divergent branch around
+                // the call cost 20 cycles per band); the other lanes pass k-mer 0
+                // and event 0 of the read, which exist because the bad lane's cell
+                // does, and drop the result.
+                const int64_t ko = r.km_off + (bad ? k0 + o : 0);
+                const SlowCell c = slow_cell_call(lp, s1, left, a.ev_mean[r.ev_off + (bad ? e0 - o : 0)], a.km_gm[ko],
+                                                  a.km_sd[ko], a.km_k1[ko], cc.lp_step, cc.lp_stay, cc.lp_skip);
+                best = bad ? c.best : best;
+                from = bad ? c.from : from;
+                slow += bad ? 1 : 0;
             }
             best = valid ? best : -INFINITY;
             from = valid ? from : 0u;

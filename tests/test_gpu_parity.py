@@ -125,9 +125,13 @@ def test_single_read_drop_in(lib, oracle_mod, dump_subset):
         assert np.array_equal(p, golden[i])
 
 
-def test_fp64_fallback_cells_stay_exact(lib, oracle_mod):
+@pytest.mark.parametrize("shape", ["warp", "wide", "medium"])
+def test_fp64_fallback_cells_stay_exact(lib, oracle_mod, shape):
     """A pore model with level_stdv near 0.4 makes emissions tiny, which defeats
-    the FP32 exactness proof and sends many cells down the FP64 path."""
+    the FP32 exactness proof and sends many cells down the FP64 path: on the
+    warp shape, and on the wide and medium shapes, which redo a band's unproven
+    cells after the band's closing barrier (every score and backpointer of the
+    longest read checked)."""
     from abea_gb300 import synth
     rng = np.random.default_rng(17)
     model = synth.make_model(rng)
@@ -140,12 +144,24 @@ def test_fp64_fallback_cells_stay_exact(lib, oracle_mod):
         evs.append(e)
         scs.append((1.0, 0.0, 1.0, 0.0))
     batch = abea.from_reads(seqs, evs, np.array(scs, dtype=abea.types.SCALINGS_DTYPE), model)
-    ctx = abea.Context(0, abea.MODE_PLAIN)
+    ctx = abea.Context(0, abea.MODE_PLAIN if shape == "warp" else abea.MODE_BATCHED, store_scores=True)
+    if shape == "wide":
+        ctx.set_option(abea.OPT_LONG_READ_BANDS, 1)
+    if shape == "medium":
+        ctx.set_option(abea.OPT_LONG_READ_BANDS, 1 << 40)
+        ctx.set_option(abea.OPT_MEDIUM_READ_BANDS, 1)
     dev = ctx.upload(batch)
     dev.run()
     gp, gc = dev.results()
-    op, oc, _ = oracle_batch(oracle_mod, batch)
+    op, oc, obest = oracle_batch(oracle_mod, batch)
     assert_same_alignments(batch, gp, gc, op, oc)
+    assert np.array_equal(dev.best_scores().view(np.uint32), obest.view(np.uint32))
+    b, t, bll = dev.read_bands(2, scores=True)
+    _, _, info = oracle_mod.align(batch.sequence(2), batch.read_events(2), batch.model,
+                                  batch.scalings[2], want_bands=True)
+    assert np.array_equal(b.view(np.uint32), info["bands"].view(np.uint32))
+    assert np.array_equal(t, info["trace"])
+    assert np.array_equal(bll, info["bll"])
     assert dev.slow_cells() > 1000
 
 
