@@ -79,6 +79,10 @@ extern "C" const char* abea_status_string(abea_status_t s) {
 extern "C" const char* abea_version(void) { return "abea-gb300 0.1 (sm_103a)"; }
 
 // ---------------------------------------------------------------- objects
+// a batch's input mirror (at 0) and output mirror (at kAuxMirror), in one device block
+constexpr size_t kAuxBytes = 64, kAuxMirror = 16;
+static_assert(sizeof(InMirror) <= kAuxMirror && kAuxMirror + sizeof(OutMirror) <= kAuxBytes, "aux layout");
+
 struct DevSlab {
     void* base = nullptr;
     size_t bytes = 0;
@@ -114,6 +118,7 @@ struct abea_batch {
     float* d_ck = nullptr;           // checkpoint records
     uint8_t* d_ck_scratch = nullptr; // one kCkBands-band trace segment per checkpointed read
     int32_t* d_spec = nullptr;       // cell maps of the wide reads' block-parallel tracebacks
+    char* d_aux = nullptr;           // [0]: the InMirror; [kAuxMirror]: the OutMirror
     int32_t* d_band_k0 = nullptr;
     abea_aligned_pair_t* d_pairs = nullptr;
     int32_t* d_n_pairs = nullptr;
@@ -160,6 +165,8 @@ struct abea_ctx {
     abea_batch* sslot[2] = {nullptr, nullptr};
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t sev[2][4] = {};  // per slot: uploaded, compute start, compute end, results copied
+    char* h_aux = nullptr;  // pinned: abea_align_batch's mirrors, then its counters and statuses
+    size_t h_aux_bytes = 0;
     std::map<uint64_t, int64_t> tuned;      // autotuned wide-shape threshold per workload signature
     std::map<uint64_t, int64_t> tuned_mid;  // autotuned medium-shape threshold per workload signature
 };
@@ -222,6 +229,7 @@ extern "C" void abea_ctx_destroy(abea_ctx_t* c) {
             if (c->sev[i][j]) cudaEventDestroy(c->sev[i][j]);
     }
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->h_aux) cudaFreeHost(c->h_aux);
     for (int i = 0; i < 8; ++i)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     for (int i = 0; i < 16; ++i)
@@ -437,7 +445,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // Carves the device slab; grows it when needed.
 static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 0) {
     size_t n = (size_t)std::max(b->n_reads, 1);
-    size_t sizes[32] = {
+    size_t sizes[33] = {
         sizeof(ReadDesc) * n,                                   // reads
         (size_t)std::max<int64_t>(b->seq_bytes, 1),             // seq
         sizeof(abea_event_t) * (size_t)std::max<int64_t>(b->n_events_total, 1),
@@ -469,8 +477,9 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
         sizeof(float) * (size_t)std::max<int64_t>(b->ck_floats, 16),  // checkpoints
         (size_t)kCkBands * kSlots * (size_t)std::max<int32_t>(b->n_ck, 0),  // recompute scratch
         sizeof(int32_t) * kSpecRound * kSpecBands * (size_t)b->n_spec,      // traceback cell maps
+        kAuxBytes,  // landed counter and output mirror
         0};
-    const int n_bufs = 31;
+    const int n_bufs = 32;
     size_t total = 0;
     for (int i = 0; i < n_bufs; ++i) total += align256(sizes[i]);
     if (total > b->slab.bytes) {
@@ -487,7 +496,7 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
         b->slab.bytes = want;
     }
     char* p = (char*)b->slab.base;
-    void* ptrs[32];
+    void* ptrs[33];
     for (int i = 0; i < n_bufs; ++i) {
         ptrs[i] = sizes[i] ? (void*)p : nullptr;
         p += align256(sizes[i]);
@@ -523,19 +532,23 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
     b->d_ck = (float*)ptrs[28];
     b->d_ck_scratch = (uint8_t*)ptrs[29];
     b->d_spec = (int32_t*)ptrs[30];
+    b->d_aux = (char*)ptrs[31];
     b->scores_kept = scores;
     b->carve.assign(1, (uint64_t)(uintptr_t)b->slab.base);
     for (int i = 0; i < n_bufs; ++i) b->carve.push_back((uint64_t)sizes[i]);
     return ABEA_OK;
 }
 
-static abea_status_t upload(abea_batch* b, const HostInputs& in, cudaStream_t st) {
+// Copies a batch to the device.  bases_events = false leaves out the bases and
+// the events (the pre stage then reads them from the caller's pinned memory).
+static abea_status_t upload(abea_batch* b, const HostInputs& in, cudaStream_t st, bool bases_events = true) {
     if (b->n_reads == 0) return ABEA_OK;
+    CUDA_TRY(cudaMemsetAsync(b->d_aux, 0, kAuxBytes, st));  // no input or output mirror
     CUDA_TRY(cudaMemcpyAsync(b->d_reads, b->reads.data(), sizeof(ReadDesc) * b->reads.size(),
                              cudaMemcpyHostToDevice, st));
-    if (b->seq_bytes > 0)
+    if (bases_events && b->seq_bytes > 0)
         CUDA_TRY(cudaMemcpyAsync(b->d_seq, in.read, (size_t)b->seq_bytes, cudaMemcpyHostToDevice, st));
-    if (b->n_events_total > 0)
+    if (bases_events && b->n_events_total > 0)
         CUDA_TRY(cudaMemcpyAsync(b->d_ev, in.event_table, sizeof(abea_event_t) * (size_t)b->n_events_total,
                                  cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(b->d_model, in.model, sizeof(abea_model_t) * ABEA_NUM_KMER,
@@ -569,8 +582,8 @@ static int64_t d2h_bytes(const abea_batch* b) {
 // 1,024-read batch of 1-10 kb reads and the 4,096-read adjoint batch: best none).
 // kWarpFloorCyc includes the warp-shape read's traceback.  Ties go to fewer wide
 // reads; the threshold is the band count of the n-th wide read (none: INT64_MAX).
+constexpr double kWideCyc = 400, kWarpFloorCyc = 1800, kWarpSmCyc = 250;
 static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
-    constexpr double kWideCyc = 400, kWarpFloorCyc = 1800, kWarpSmCyc = 250;
     const size_t n = b->order.size();
     std::vector<int64_t> wide_ok;  // band counts of the reads that may be wide, longest first
     double rest_bands = 0;
@@ -648,7 +661,7 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
     LaunchArgs la;
     const GlobalConsts g = global_consts(b->var_aware);
     la.pre = PreArgs{b->d_reads, b->n_reads, g, b->d_seq, b->d_ev, b->d_model, b->d_ev_mean, b->d_km_gm,
-                     b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col};
+                     b->d_km_sd, b->d_km_rsd, b->d_km_k1, b->d_last_col, (const InMirror*)b->d_aux};
     la.core = CoreArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_rsd, b->d_km_k1,
                        b->d_last_col, b->d_trace, b->scores_kept ? b->d_scores : nullptr, b->d_band_k0,
                        b->d_slow, b->d_order, b->d_queue, b->n_wide, b->d_ck, b->d_ck_scratch, b->d_spec,
@@ -656,7 +669,8 @@ static abea_status_t launch_all(abea_ctx* c, abea_batch* b, int* launches, bool 
                        (long long)c->spin_limit, b->n_mid};
     la.post = PostArgs{b->d_reads, b->n_reads, g, b->d_ev_mean, b->d_km_gm, b->d_km_sd, b->d_km_k1, b->d_km_rsd,
                        b->d_last_col, b->d_trace, b->d_band_k0, b->d_pairs, b->d_n_pairs, b->d_best,
-                       b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event};
+                       b->d_status, b->d_path_len, b->d_path_flags, b->d_best_event,
+                       (const OutMirror*)(b->d_aux + kAuxMirror)};
     la.sm_count = c->sm_count;
     la.stream = c->stream;
     la.ev_pre = c->ev[1];
@@ -955,20 +969,28 @@ static abea_status_t download(abea_ctx* c, abea_batch* b, abea_aligned_pair_t* p
     return ABEA_OK;
 }
 
-static abea_status_t check_status(abea_ctx* c, abea_batch* b) {
+// The batch's device-side counters and per-read statuses as a status: from
+// `host` (counters, then statuses, already copied by the caller after a
+// synchronize) or copied here.
+static abea_status_t check_status(abea_ctx* c, abea_batch* b, const void* host = nullptr) {
     if (b->n_reads == 0) return ABEA_OK;
-    unsigned long long cnt[4] = {0, 0, 0, 0};
-    CUDA_TRY(cudaMemcpyAsync(cnt, b->d_slow, sizeof(cnt), cudaMemcpyDeviceToHost, c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    std::vector<char> buf;
+    if (!host) {
+        buf.resize(sizeof(unsigned long long) * 4 + sizeof(int32_t) * (size_t)b->n_reads);
+        CUDA_TRY(cudaMemcpyAsync(buf.data(), b->d_slow, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost,
+                                 c->stream));
+        CUDA_TRY(cudaMemcpyAsync(buf.data() + sizeof(unsigned long long) * 4, b->d_status,
+                                 sizeof(int32_t) * (size_t)b->n_reads, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        host = buf.data();
+    }
+    unsigned long long cnt[4];
+    memcpy(cnt, host, sizeof(cnt));
     if (cnt[2]) return fail(ABEA_ERR_TIMEOUT, "%llu device-side waits ran out of polls (ABEA_OPT_SPIN_LIMIT)", cnt[2]);
     if (cnt[3]) return fail(ABEA_ERR_INTERNAL, "%llu device-side stores out of their region (bounds-checked build)", cnt[3]);
-    std::vector<int32_t> st((size_t)b->n_reads);
-    CUDA_TRY(cudaMemcpyAsync(st.data(), b->d_status, sizeof(int32_t) * st.size(), cudaMemcpyDeviceToHost,
-                             c->stream));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
-    for (size_t i = 0; i < st.size(); ++i)
-        if (st[i] != 0)
-            return fail((abea_status_t)st[i], "read %zu: %s", i, abea_status_string((abea_status_t)st[i]));
+    const int32_t* st = (const int32_t*)((const char*)host + sizeof(cnt));
+    for (int32_t i = 0; i < b->n_reads; ++i)
+        if (st[i] != 0) return fail((abea_status_t)st[i], "read %d: %s", i, abea_status_string((abea_status_t)st[i]));
     return ABEA_OK;
 }
 
@@ -1256,6 +1278,25 @@ extern "C" abea_status_t abea_batch_recalibrate(abea_ctx_t* c, abea_batch_t* b, 
 }
 
 // ---------------------------------------------------------------- one-call batch
+// The caller's host buffer of `bytes` bytes as the device sees it: pinned memory
+// is mapped into every device's address space under unified addressing.  Both
+// ends must be pinned and mapped contiguously; otherwise (pageable memory)
+// nullptr.
+static void* device_view(void* p, size_t bytes) {
+    if (!p || bytes == 0) return nullptr;
+    auto view = [](void* q) -> char* {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return at.type == cudaMemoryTypeHost ? (char*)at.devicePointer : nullptr;
+    };
+    char* first = view(p);
+    char* last = view((char*)p + bytes - 1);
+    return first && last == first + bytes - 1 ? first : nullptr;
+}
+
 static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_aligned_pair_t* pairs,
                                       int32_t* n_pairs) {
     NvtxRange nv("abea align_batch");
@@ -1269,12 +1310,54 @@ static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_al
     }
     abea_batch* b = c->scratch;
     if ((st = plan(b, in, (int)c->var_aware, c->trace_budget)) || (st = ensure_device(b, c->store_scores != 0))) return st;
+    // Pinned buffers of the caller are used in place: the pre stage reads each
+    // read's bases and events from host memory (no input copy precedes the
+    // kernel), and each read's pairs and count go into the caller's buffers as
+    // the read finishes (no result copy follows it).  Pageable buffers are copied.
+    InMirror im{nullptr, nullptr};
+    OutMirror om{nullptr, nullptr};
+    if (b->n_reads > 0) {
+        if (b->seq_bytes > 0 && b->n_events_total > 0)
+            im = InMirror{(const char*)device_view((void*)in.read, (size_t)b->seq_bytes),
+                          (const abea_event_t*)device_view((void*)in.event_table,
+                                                           sizeof(abea_event_t) * (size_t)b->n_events_total)};
+        if (!im.seq || !im.ev) im = InMirror{nullptr, nullptr};
+        om = OutMirror{(abea_aligned_pair_t*)device_view(pairs, sizeof(abea_aligned_pair_t) * (size_t)b->pair_cap),
+                       (int32_t*)device_view(n_pairs, sizeof(int32_t) * (size_t)b->n_reads)};
+    }
+    const bool mirror = im.seq || om.pairs || om.n_pairs;
+    // pinned: the mirrors as copied to the device, then the batch's counters and
+    // statuses as copied back (read before the call returns, after one synchronize)
+    const size_t aux_bytes = kAuxBytes + sizeof(unsigned long long) * 4 + sizeof(int32_t) * (size_t)b->n_reads;
+    if (c->h_aux_bytes < aux_bytes) {
+        if (c->h_aux) cudaFreeHost(c->h_aux);
+        c->h_aux = nullptr;
+        c->h_aux_bytes = 0;
+        if (cudaHostAlloc((void**)&c->h_aux, aux_bytes, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            c->h_aux = nullptr;
+            return fail(ABEA_ERR_OUT_OF_MEMORY, "pinned host allocation failed");
+        }
+        c->h_aux_bytes = aux_bytes;
+    }
     CUDA_TRY(cudaEventRecord(c->ev[4], c->stream));
-    if ((st = upload(b, in, c->stream))) return st;
+    if ((st = upload(b, in, c->stream, im.seq == nullptr))) return st;
+    if (mirror) {
+        memset(c->h_aux, 0, kAuxBytes);
+        memcpy(c->h_aux, &im, sizeof(im));
+        memcpy(c->h_aux + kAuxMirror, &om, sizeof(om));
+        CUDA_TRY(cudaMemcpyAsync(b->d_aux, c->h_aux, kAuxBytes, cudaMemcpyHostToDevice, c->stream));
+    }
     CUDA_TRY(cudaEventRecord(c->ev[5], c->stream));
     if ((st = run_batch(c, b))) return st;
     CUDA_TRY(cudaEventRecord(c->ev[6], c->stream));
-    if ((st = download(c, b, pairs, n_pairs))) return st;
+    if ((st = download(c, b, om.pairs ? nullptr : pairs, om.n_pairs ? nullptr : n_pairs))) return st;
+    char* hst = c->h_aux + kAuxBytes;
+    if (b->n_reads > 0) {
+        CUDA_TRY(cudaMemcpyAsync(hst, b->d_slow, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(hst + sizeof(unsigned long long) * 4, b->d_status, sizeof(int32_t) * (size_t)b->n_reads,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    }
     CUDA_TRY(cudaEventRecord(c->ev[7], c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
     if ((st = collect_timing(c, b))) return st;
@@ -1283,7 +1366,7 @@ static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_al
     b->timing.h2d_ms = t;
     CUDA_TRY(cudaEventElapsedTime(&t, c->ev[6], c->ev[7]));
     b->timing.d2h_ms = t;
-    return check_status(c, b);
+    return check_status(c, b, hst);
 }
 
 extern "C" abea_status_t abea_align_batch(abea_ctx_t* c, int32_t n_reads, const char* read,

@@ -93,39 +93,76 @@ __device__ __forceinline__ CellConsts make_consts(const ReadDesc& r, const Globa
 // Pre of read i by nt cooperating threads (thread index t): the read's k-mer
 // parameters, event means and last-column initialisation.  The batched form runs
 // it in the block or warp that fills the read, just before the fill.
+//
+// The bases and events come from HBM, or, when the caller's buffers are pinned
+// (a.inm), straight from host memory over the CPU-GPU link: no copy of the
+// inputs precedes the kernel, and every read's pre stage loads its own.  A thread
+// takes kPreUnroll positions per pass with every load issued before any use
+// (indexes clamped into the read), so that several round trips to host memory
+// are in flight at once.
+constexpr int kPreUnroll = 4;
 __device__ __forceinline__ void pre_read(const PreArgs& a, int i, int t, int nt) {
     const ReadDesc r = a.reads[i];
     if (r.skip) return;
-    const char* s = a.seq + r.seq_off;
+    const InMirror* m = a.inm;
+    const char* seq = a.seq;
+    const abea_event_t* ev_in = a.ev_in;
+    if (m) {
+        const InMirror mv = *m;
+        if (mv.seq) seq = mv.seq;
+        if (mv.ev) ev_in = mv.ev;
+    }
+    const char* s = seq + r.seq_off;
     const int nk = r.n_kmers, nk_pad = round_up_dev(nk);
-    for (int k = t; k < nk_pad; k += nt) {
-        float gm = 0.f, sd = 1.f, rsd = 1.f, k1 = 0.f;
-        if (k < nk) {
-            uint32_t rank = 0;
+    for (int k0 = t; k0 < nk_pad; k0 += kPreUnroll * nt) {
+        char base[kPreUnroll][ABEA_KMER_SIZE];
 #pragma unroll
-            for (int j = 0; j < ABEA_KMER_SIZE; ++j) rank = (rank << 2) | base_rank(s[k + j]);
-            abea_model_t m = a.model[rank];
-            // gp_mean = scale*level_mean + shift; gp_stdv = level_stdv (scaling.var is
-            // ignored by the reference, GPU/align_cuda.cl:509); cached log stdv.
-            gm = __fadd_rn(__fmul_rn(r.scale, m.level_mean), r.shift);
-            sd = m.level_stdv;
-            float lsd = m.level_log_stdv;
-            if (a.g.var_aware) {
-                sd = __fmul_rn(sd, r.var);
-                lsd = __fadd_rn(lsd, r.log_var);
-            }
-            rsd = __frcp_rn(sd);
-            k1 = __fsub_rn(kLogInvSqrt2Pi, lsd);
+        for (int u = 0; u < kPreUnroll; ++u) {
+            const int kc = min(k0 + u * nt, nk - 1);  // nk >= 1: the read is not skipped
+#pragma unroll
+            for (int j = 0; j < ABEA_KMER_SIZE; ++j) base[u][j] = s[kc + j];
         }
-        a.km_gm[r.km_off + k] = gm;
-        a.km_sd[r.km_off + k] = sd;
-        a.km_rsd[r.km_off + k] = rsd;
-        a.km_k1[r.km_off + k] = k1;
+#pragma unroll
+        for (int u = 0; u < kPreUnroll; ++u) {
+            const int k = k0 + u * nt;
+            if (k >= nk_pad) break;
+            float gm = 0.f, sd = 1.f, rsd = 1.f, k1 = 0.f;
+            if (k < nk) {
+                uint32_t rank = 0;
+#pragma unroll
+                for (int j = 0; j < ABEA_KMER_SIZE; ++j) rank = (rank << 2) | base_rank(base[u][j]);
+                abea_model_t mm = a.model[rank];
+                // gp_mean = scale*level_mean + shift; gp_stdv = level_stdv (scaling.var is
+                // ignored by the reference, GPU/align_cuda.cl:509); cached log stdv.
+                gm = __fadd_rn(__fmul_rn(r.scale, mm.level_mean), r.shift);
+                sd = mm.level_stdv;
+                float lsd = mm.level_log_stdv;
+                if (a.g.var_aware) {
+                    sd = __fmul_rn(sd, r.var);
+                    lsd = __fadd_rn(lsd, r.log_var);
+                }
+                rsd = __frcp_rn(sd);
+                k1 = __fsub_rn(kLogInvSqrt2Pi, lsd);
+            }
+            a.km_gm[r.km_off + k] = gm;
+            a.km_sd[r.km_off + k] = sd;
+            a.km_rsd[r.km_off + k] = rsd;
+            a.km_k1[r.km_off + k] = k1;
+        }
     }
     const int ne = r.n_events, ne_pad = round_up_dev(ne);
-    for (int e = t; e < ne_pad; e += nt) {
-        a.ev_mean[r.ev_off + e] = e < ne ? a.ev_in[r.ev_src + e].mean : 0.f;
-        a.last_col[r.ev_off + e] = -INFINITY;
+    const abea_event_t* ev = ev_in + r.ev_src;
+    for (int e0 = t; e0 < ne_pad; e0 += kPreUnroll * nt) {
+        float mean[kPreUnroll];
+#pragma unroll
+        for (int u = 0; u < kPreUnroll; ++u) mean[u] = ev[min(e0 + u * nt, ne - 1)].mean;  // ne >= 1
+#pragma unroll
+        for (int u = 0; u < kPreUnroll; ++u) {
+            const int e = e0 + u * nt;
+            if (e >= ne_pad) break;
+            a.ev_mean[r.ev_off + e] = e < ne ? mean[u] : 0.f;
+            a.last_col[r.ev_off + e] = -INFINITY;
+        }
     }
 }
 
@@ -1436,12 +1473,23 @@ __device__ void post_tail(const CoreArgs& ca, const PostArgs& a, int ri, const R
                           int last_from);
 
 // `ring`: kRing * 2 KB of shared memory (16-byte aligned) for the traceback's trace chunks.
+// A finished read's pairs out[0, n) into the caller's host buffer, when the batch
+// mirrors its results there (threads t of nt; the pairs are final and visible to them).
+__device__ __forceinline__ void mirror_pairs(const PostArgs& a, const ReadDesc& r, const abea_aligned_pair_t* out,
+                                             int n, int t, int nt) {
+    abea_aligned_pair_t* h = a.outm ? a.outm->pairs : nullptr;
+    if (!h || n <= 0) return;
+    h += r.out_off;
+    for (int i = t; i < n; i += nt) h[i] = out[i];
+}
+
 template <int kRing>
 __device__ void post_read_warp(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* ring, Rings& rg, int lane) {
     const ReadDesc r = a.reads[ri];
     if (r.skip) {
         if (lane == 0) {
             a.n_pairs[ri] = 0;
+            if (a.outm && a.outm->n_pairs) a.outm->n_pairs[ri] = 0;
             a.best_scores[ri] = -INFINITY;
             a.status[ri] = 0;
         }
@@ -1585,6 +1633,8 @@ __device__ void post_tail(const CoreArgs& ca, const PostArgs& a, int ri, const R
             }
             result = n_out;
             reversed = true;
+            __syncwarp();
+            mirror_pairs(a, r, out, n_out, lane, 32);
         }
     } else if (status != 0) {
         result = status;
@@ -1598,6 +1648,7 @@ __device__ __forceinline__ void post_write(const PostArgs& a, int ri, int result
                                            int n_out, int cap, bool reversed, int last_from) {
     {
         a.n_pairs[ri] = result;
+        if (a.outm && a.outm->n_pairs) a.outm->n_pairs[ri] = result;
         a.best_scores[ri] = best;
         a.status[ri] = status;
         if (a.path_len) {
@@ -1910,6 +1961,10 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
             out[i] = y;
             out[n_out - 1 - i] = x;
         }
+    if (pass && a.outm) {
+        __syncthreads();  // the reversal is done
+        mirror_pairs(a, r, out, n_out, t, kWideThreads);
+    }
     if (t == 0) post_write(a, ri, pass ? n_out : 0, best, best_e, 0, n_out, cap, pass, last_from);
 }
 

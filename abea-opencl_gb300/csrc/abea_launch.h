@@ -11,6 +11,13 @@ extern "C" const char* abea_internal_set_error(const char* msg);
 
 namespace abea {
 
+// Pinned host memory of abea_align_batch's caller that the pre stage reads each
+// read's bases and events from (device-mapped; no copy to HBM first), or nulls.
+struct InMirror {
+    const char* seq;
+    const abea_event_t* ev;
+};
+
 struct PreArgs {
     const ReadDesc* reads;
     int n_reads;
@@ -24,6 +31,7 @@ struct PreArgs {
     float* km_rsd;
     float* km_k1;
     float* last_col;
+    const InMirror* inm;  // nullptr, or a device copy of the input mirror
 };
 
 struct CoreArgs {
@@ -51,6 +59,13 @@ struct CoreArgs {
     int32_t n_mid;                 // the reads after the wide ones that run on the medium shape (batched form)
 };
 
+// Host memory the kernels write each read's results into as the read finishes
+// (device-mapped pinned buffers of abea_align_batch's caller), or nulls.
+struct OutMirror {
+    abea_aligned_pair_t* pairs;  // the caller's event_align_pairs
+    int32_t* n_pairs;            // the caller's n_event_align_pairs
+};
+
 struct PostArgs {
     const ReadDesc* reads;
     int n_reads;
@@ -70,6 +85,7 @@ struct PostArgs {
     int32_t* path_len;    // optional (nullptr): path length, for the adjoint
     int32_t* path_flags;  // kPath* bits | move into the last walked cell << 8
     int32_t* best_event;  // event of the best end
+    const OutMirror* outm;  // nullptr, or a device copy of the mirror (batched form)
 };
 
 constexpr int32_t kPathReversed = 1, kPathTruncated = 2, kPathNoEnd = 4, kPathError = 8;

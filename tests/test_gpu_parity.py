@@ -382,3 +382,46 @@ def test_autotuner_cache_round_trip(lib, tmp_path):
     sig, wide = lines[1].split()[:2]
     (tmp_path / "v1.txt").write_text(f"abea-autotune 1 sm_count {sm}\n{sig} {wide}\n")
     assert other.autotune_load(str(tmp_path / "v1.txt")) == 1
+
+
+def _pinned_call(ctx, batch):
+    """abea_align_batch on pinned copies of the batch into pinned outputs filled
+    with a pattern (so every count and pair of the result must be written)."""
+    pb = abea.pin_batch(batch)
+    pairs = abea.pinned_empty(max(batch.pair_capacity(), 1), abea.types.PAIR_DTYPE)
+    counts = abea.pinned_empty(batch.n_reads, np.int32)
+    pairs.view(np.uint8)[:] = 0xA5
+    counts[:] = -7
+    return ctx.align_batch(pb, out_pairs=pairs, out_counts=counts)
+
+
+@pytest.mark.parametrize("workload,mode", [("f5c_batch", abea.MODE_BATCHED), ("uneven", abea.MODE_BATCHED),
+                                           ("f5c_batch", abea.MODE_PLAIN)])
+def test_align_batch_pinned_inputs_and_results_in_place(lib, workload, mode):
+    """abea_align_batch with pinned buffers: the pre stage reads every read's
+    bases and events from host memory (no input copy) and each read's
+    AlignedPairs and count go into the caller's buffers as the read finishes (no
+    result copy).  Results equal the device-resident batch's, in both forms, on
+    the second call (graph replay) too, and with pageable buffers."""
+    from abea_gb300 import synth
+    batch = synth.make_batch(workload, seed=1)
+    ctx = abea.Context(0, mode)
+    dev = ctx.upload(batch)
+    dev.run()
+    rp, rc = dev.results()
+    dev.close()
+    for _ in range(2):
+        gp, gc = _pinned_call(ctx, batch)
+        assert_same_alignments(batch, gp, gc, rp, rc)
+    up, uc = ctx.align_batch(batch)
+    assert_same_alignments(batch, up, uc, rp, rc)
+
+
+def test_pinned_results_on_the_edge_cases(lib, oracle_mod, ref_synthetic):
+    """Pinned outputs with reads that are skipped (shorter than a k-mer, no
+    events), fail QC or overflow: every count is written, the pairs match."""
+    batch = ref_synthetic[0]
+    op, oc, _ = oracle_batch(oracle_mod, batch)
+    for mode in (abea.MODE_PLAIN, abea.MODE_BATCHED):
+        gp, gc = _pinned_call(abea.Context(0, mode), batch)
+        assert_same_alignments(batch, gp, gc, op, oc)
