@@ -102,7 +102,11 @@ def make_read(rng, model, length, scale, shift, var, skip_p=0.05, mean_events=1.
 
 def make_batch(workload: str = "small", seed: int = 1, perturb: bool = False, lengths=None) -> Batch:
     """A flattened synthetic batch.  `perturb` (adjoint workload) returns
-    scalings offset from the truth by shift +-8 pA and scale +-10%."""
+    scalings offset from the truth by shift +-8 pA and scale +-10%.  "f5c_longest"
+    is the f5c batch's longest read alone (its band chain sets the batch's time)."""
+    if workload == "f5c_longest":
+        full = make_batch("f5c_batch", seed=seed, perturb=perturb)
+        return full.subset(np.array([int(np.argmax(full.n_bands()))]))
     rng = np.random.default_rng(seed)
     model = make_model(rng)
     lens = np.asarray(lengths if lengths is not None else read_lengths(rng, workload), dtype=np.int64)

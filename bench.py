@@ -51,6 +51,7 @@ WORKLOADS = {
     "uneven": "1.3 Mbases: 80% of reads U(200 b, 5 kb), 20% U(20 kb, 100 kb)",
     "small": "64 reads, U(1 kb, 3 kb)",
     "reads1024": "1,024 reads, U(1 kb, 10 kb) (fewer reads than warps: the throughput regime's latency-bound end)",
+    "f5c_longest": "the f5c batch's longest read alone (54,382 bands at seed 1): the wide shape's band chain",
 }
 
 
@@ -201,12 +202,16 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def measured_traffic_per_cell():
-    """DRAM bytes per band cell of the core kernel from the committed ncu summary."""
+def measured_traffic_per_cell(workload: str, mode: str):
+    """DRAM bytes per band cell, and the instruction count, of one launch of the
+    batched kernel on this workload, from the committed ncu summary (None when
+    the summary has no capture of this workload and form)."""
     p = os.path.join(ROOT, "profiles", "core_dram_bytes.json")
     try:
         with open(p) as f:
-            d = json.load(f)
+            d = json.load(f)["workloads"][workload]
+        if mode != "batched":
+            return None, None
         return float(d["dram_bytes_per_band_cell"]), d
     except (OSError, KeyError, ValueError):
         return None, None
@@ -653,7 +658,7 @@ def ours(args, dist):
     peak, peak_kind = measured_peak_hbm()
     core_ms = statistics.mean(core)
     achieved = BYTES_PER_CELL * cells / (core_ms / 1e3) / 1e9
-    tpc, tinfo = measured_traffic_per_cell()
+    tpc, tinfo = measured_traffic_per_cell(args.workload, args.mode)
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                        "frac": achieved / peak, "peak_kind": f"{peak_kind} (hbm_gbs)",
                        "traffic": (tpc * cells) if tpc else None,
