@@ -475,7 +475,7 @@ def heuristic_wide_reads(n_bands, blocks: int) -> int:
     thr = f(b.ctypes.data, len(b), int(blocks))
     if thr < 0:
         raise AbeaError(-1, "abea_internal_wide_threshold: bad argument")
-    return 0 if thr >= 2**62 else int(min(np.sum(b >= thr), blocks))
+    return 0 if thr >= 2**62 else int(np.sum(b >= thr))
 
 
 def version() -> str:

@@ -428,7 +428,10 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, in
     int32_t n_spec = 0;
     for (const ReadDesc& r : b->reads)
         if (!r.skip && !r.ck && r.n_bands >= kSpecMinBands) ++n_spec;
-    b->n_spec = std::min(n_spec, kSpecMaxSlots);
+    // one scratch slot per block of the batched kernel (a block walks one wide read at a time)
+    const int grid = b->ctx ? std::max(batched_blocks_per_sm(false), batched_blocks_per_sm(true)) * b->ctx->sm_count
+                            : kSpecMaxSlots;
+    b->n_spec = n_spec > 0 ? std::min(std::max(grid, 1), kSpecMaxSlots) : 0;
     b->pair_cap = 2 * ev_end;
     b->band_cells = cells;
     // longest first; ties by index
@@ -569,20 +572,29 @@ static int64_t d2h_bytes(const abea_batch* b) {
     return (int64_t)sizeof(abea_aligned_pair_t) * b->pair_cap + (int64_t)sizeof(int32_t) * b->n_reads;
 }
 
-// Heuristic wide-shape threshold: the number n of wide reads (the longest ones
-// whose trace is kept, at most one per block) that minimises an estimate of the
-// batch's makespan, in cycles:
+// Heuristic wide-shape threshold.  First, the number n of wide reads (the longest
+// ones whose trace is kept, at most one per block, the other blocks taking the
+// warp-shape reads from the start) that minimises an estimate of the batch's
+// makespan, in cycles:
 //   the longest wide read on the wide shape, kWideCyc per band;
 //   the longest warp-shape read: kWarpFloorCyc per band, or kWarpSmCyc per band
 //     times the warps sharing its SM in the first wave (the blocks without a
 //     wide read share the other reads round-robin, at most 16 warps each);
 //   the warp-shape work spread over those blocks, kWarpSmCyc per band per SM.
-// Calibrated on GB300 by sweeping the number of wide reads (the f5c batch at two
-// seeds: best 80-100 wide reads, 10.19 ms; the uneven batch: best 20-24; a
-// 1,024-read batch of 1-10 kb reads and the 4,096-read adjoint batch: best none).
-// kWarpFloorCyc includes the warp-shape read's traceback.  Ties go to fewer wide
-// reads; the threshold is the band count of the n-th wide read (none: INT64_MAX).
-constexpr double kWideCyc = 400, kWarpFloorCyc = 1800, kWarpSmCyc = 250;
+// Then every read on the wide shape, the blocks pulling them longest first: the
+// longest read at kWideCyc per band, or all the bands over the blocks at
+// kWideSmCyc per band per block.  That wins when it is within 2% of the first
+// (it cannot be shorter than the longest read, which bounds both), except with
+// checkpointed reads, which run on the warp shape and would start last.
+// Calibrated on GB300 by sweeping the number of wide reads: the f5c batch and the
+// 1,024-read batch of 1-10 kb reads are fastest with every read wide (8.46 and
+// 18.5 ms, against 8.49-9.10 and 20.8 at the best one-per-block split); the
+// 4,096-read adjoint batch with none (35.5 ms; 68.5 with every read wide: at 27
+// reads per SM the warp shape's 16 warps issue more per SM).  kWarpFloorCyc
+// includes the warp-shape read's traceback, kWideSmCyc the wide reads' tracebacks
+// and the blocks' tail.  Ties go to fewer wide reads; the threshold is the band
+// count of the n-th wide read (every read: 1; none: INT64_MAX).
+constexpr double kWideCyc = 400, kWarpFloorCyc = 1800, kWarpSmCyc = 250, kWideSmCyc = 380;
 static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
     const size_t n = b->order.size();
     std::vector<int64_t> wide_ok;  // band counts of the reads that may be wide, longest first
@@ -592,6 +604,8 @@ static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
         rest_bands += (double)r.n_bands;
         if (!r.ck) wide_ok.push_back(r.n_bands);
     }
+    const double all_bands = rest_bands;
+    const bool any_ck = wide_ok.size() < n;
     const int max_wide = (int)std::min<size_t>(wide_ok.size(), (size_t)std::max(0, blocks - 1));
     double best_t = 0;
     int best_n = 0;
@@ -625,14 +639,19 @@ static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
             best_n = k;
         }
     }
+    if (!any_ck && !wide_ok.empty()) {
+        const double t_all = std::max((double)wide_ok[0] * kWideCyc, all_bands * kWideSmCyc / std::max(blocks, 1));
+        if (t_all <= best_t * 1.02) return 1;
+    }
     return best_n > 0 ? wide_ok[(size_t)best_n - 1] : INT64_MAX;
 }
 
 // Reads of the batched form that run on the wide and the medium shapes: the
 // longest reads over the wide threshold (the option, the autotuned value, or the
-// heuristic above), at most one per resident block, then the longest remaining
-// reads over the medium threshold (none without one; never with the cluster
-// pair); never a checkpointed read.  Fills b->dev_order with the wide reads, the
+// heuristic above; the blocks take them longest first, one at a time, as many
+// each as the queue holds; with the cluster pair at most one per cluster), then
+// the longest remaining reads over the medium threshold (none without one; never
+// with the cluster pair); never a checkpointed read.  Fills b->dev_order with the wide reads, the
 // medium reads, then the rest, each longest first, and sets n_wide and n_mid.
 static void choose_shape_reads(abea_batch* b, int sm_count, int64_t threshold, int64_t mid_threshold, bool scores,
                                bool cluster) {
@@ -642,7 +661,7 @@ static void choose_shape_reads(abea_batch* b, int sm_count, int64_t threshold, i
     std::vector<int32_t> wide, mid, rest;
     for (int32_t i : b->order) {
         const ReadDesc& r = b->reads[(size_t)i];
-        if ((int)wide.size() < blocks && !r.ck && r.n_bands >= threshold)
+        if ((!cluster || (int)wide.size() < blocks) && !r.ck && r.n_bands >= threshold)
             wide.push_back(i);
         else if (!r.ck && r.n_bands >= mid_threshold)
             mid.push_back(i);
@@ -789,8 +808,9 @@ static abea_status_t run_batch(abea_ctx* c, abea_batch* b) {
 
 // Autotuner: times the batched form on `b` with candidate thresholds for the
 // wide shape — none, the heuristic, the band counts of the reads ranked at 1, 2,
-// 3, 4, 6, 8, 12 and 16 sixteenths of the resident blocks, and 15, 20, 45 and 60%
-// of the longest read — keeps the fastest for
+// 3, 4, 6, 8, 12 and 16 sixteenths of the resident blocks and at 3/2, 2, 3, 4 and
+// 6 times their number (every read when the batch has fewer), and 15, 20, 45 and
+// 60% of the longest read — keeps the fastest for
 // this workload signature (longest read, read count and total bands, log2
 // buckets) and returns it.
 extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* best_threshold, float* best_ms) {
@@ -798,12 +818,17 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
     if (!c || !b) return fail(ABEA_ERR_INVALID_ARG, "abea_autotune: null argument");
     if (b->n_reads == 0) return ABEA_OK;
     const abea_mode_t mode0 = c->mode;
-    const int64_t thr0 = c->long_read_bands;
+    const int64_t thr0 = c->long_read_bands, mid0 = c->mid_read_bands;
     c->mode = ABEA_MODE_BATCHED;
+    // the wide stage runs without medium reads: neither the option nor a medium
+    // threshold tuned earlier for this signature may shape its timings
+    c->mid_read_bands = INT64_MAX;
     const int blocks = batched_blocks_per_sm(b->scores_kept) * c->sm_count;
     int64_t longest = 0;
     for (const ReadDesc& r : b->reads) longest = std::max<int64_t>(longest, r.n_bands);
     std::vector<int64_t> cands = {INT64_MAX, heuristic_threshold(b, blocks)};
+    if (c->wide_cluster == 0 && std::find(cands.begin(), cands.end(), (int64_t)1) == cands.end())
+        cands.push_back(1);  // every read wide
     for (int num : {1, 2, 3, 4, 6, 8, 12, 16}) {  // the longest num/16 of the resident blocks
         size_t k = std::min<size_t>(b->order.size(), (size_t)std::max(1, blocks * num / 16)) - 1;
         const int64_t c = std::max<int64_t>(1, b->reads[(size_t)b->order[k]].n_bands);
@@ -813,6 +838,12 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
         const int64_t c = std::max<int64_t>(1, longest * pct / 100);
         if (std::find(cands.begin(), cands.end(), c) == cands.end()) cands.push_back(c);
     }
+    if (c->wide_cluster == 0)
+        for (int mul : {3, 4, 6, 8, 12}) {  // more wide reads than blocks: 3/2 .. 6 per block, then every read
+            const size_t k = std::min<size_t>(b->order.size(), (size_t)blocks * mul / 2);
+            const int64_t v = k < b->order.size() ? std::max<int64_t>(1, b->reads[(size_t)b->order[k - 1]].n_bands) : 1;
+            if (std::find(cands.begin(), cands.end(), v) == cands.end()) cands.push_back(v);
+        }
     int64_t best = 0;
     float best_t = 1e30f;
     abea_status_t st = ABEA_OK;
@@ -833,7 +864,6 @@ extern "C" abea_status_t abea_autotune(abea_ctx_t* c, abea_batch_t* b, int64_t* 
     // then the medium shape with that wide threshold: none, or the band count of
     // the reads that leave k of the remaining reads for it (k from a quarter of the
     // block halves to four per half) or at fractions of the longest remaining read
-    const int64_t mid0 = c->mid_read_bands;
     int64_t best_mid = INT64_MAX;
     if (!st && c->wide_cluster == 0) {
         c->long_read_bands = best;

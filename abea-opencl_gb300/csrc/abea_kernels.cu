@@ -97,10 +97,11 @@ __device__ __forceinline__ CellConsts make_consts(const ReadDesc& r, const Globa
 // The bases and events come from HBM, or, when the caller's buffers are pinned
 // (a.inm), straight from host memory over the CPU-GPU link: no copy of the
 // inputs precedes the kernel, and every read's pre stage loads its own.  A thread
-// takes kPreUnroll positions per pass with every load issued before any use
-// (indexes clamped into the read), so that several round trips to host memory
-// are in flight at once.
-constexpr int kPreUnroll = 4;
+// takes kPreUnroll k-mer positions (kEvUnroll events) per pass with every load
+// issued before any use (indexes clamped into the read), so that many round trips
+// to host memory are in flight at once: a warp-shape read's pre stage is latency-
+// bound on them (a k-mer's six bases share the cache lines of its neighbours').
+constexpr int kPreUnroll = 4, kEvUnroll = 16;
 __device__ __forceinline__ void pre_read(const PreArgs& a, int i, int t, int nt) {
     const ReadDesc r = a.reads[i];
     if (r.skip) return;
@@ -152,12 +153,12 @@ __device__ __forceinline__ void pre_read(const PreArgs& a, int i, int t, int nt)
     }
     const int ne = r.n_events, ne_pad = round_up_dev(ne);
     const abea_event_t* ev = ev_in + r.ev_src;
-    for (int e0 = t; e0 < ne_pad; e0 += kPreUnroll * nt) {
-        float mean[kPreUnroll];
+    for (int e0 = t; e0 < ne_pad; e0 += kEvUnroll * nt) {
+        float mean[kEvUnroll];
 #pragma unroll
-        for (int u = 0; u < kPreUnroll; ++u) mean[u] = ev[min(e0 + u * nt, ne - 1)].mean;  // ne >= 1
+        for (int u = 0; u < kEvUnroll; ++u) mean[u] = ev[min(e0 + u * nt, ne - 1)].mean;  // ne >= 1
 #pragma unroll
-        for (int u = 0; u < kPreUnroll; ++u) {
+        for (int u = 0; u < kEvUnroll; ++u) {
             const int e = e0 + u * nt;
             if (e >= ne_pad) break;
             a.ev_mean[r.ev_off + e] = e < ne ? mean[u] : 0.f;
@@ -1743,7 +1744,7 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
                 }
             ps.best = b;
             ps.best_e = b > -INFINITY ? be : 0;
-            ps.slot = b > -INFINITY ? atomicAdd(&ca.queue[2], 1) : 0;  // a scratch slot for the maps
+            ps.slot = blockIdx.x;  // the block's scratch slot for the maps (one wide read at a time)
         }
     }
     __syncthreads();
@@ -2036,8 +2037,9 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         sm.free_rank = q < a.n_wide + n_midb ? -1 : q - a.n_wide - n_midb;
     }
     __syncthreads();
-    const int wide_read = sm.pick, free_rank = sm.free_rank;
-    if (wide_read >= 0) {
+    int wide_read = sm.pick;
+    const int free_rank = sm.free_rank;
+    while (wide_read >= 0) {
         const ReadDesc& r = a.reads[wide_read];
         pre_read(pa, wide_read, t, kWideThreads);
         __syncthreads();  // the read's parameters are in memory for the whole block
@@ -2046,12 +2048,19 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         __threadfence_block();
         // the whole block walks the wide read's traceback (the fill's shared memory is free)
         post_wide_block(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0], t);
+        // then the next wide read past the first wave (one per block), longest first
+        __syncthreads();  // the traceback is done with the block's shared memory and the pick
+        if (t == 0) {
+            const int q = (int)gridDim.x + atomicAdd(&a.queue[4], 1);
+            sm.pick = q < a.n_wide ? a.order[q] : -1;
+        }
+        __syncthreads();
+        wide_read = sm.pick;
     }
     // phase 1b: the medium reads, each half of a medium block (eight warps) pulling
     // one at a time: pre, fill, and the traceback by the half's first warp; the
-    // blocks done with a wide read join in
+    // blocks done with their wide reads join in
     if (a.n_mid > 0 && free_rank < 0) {
-        if (wide_read >= 0) __syncthreads();  // the wide read's traceback is done with its memory
         const int half = warp >> 3, ht = t & (kMidThreads - 1), hw = ht >> 5;
         MidSmem& ms = *reinterpret_cast<MidSmem*>(&sm.post[half * (kBatchedWarps / 2)]);
         const int bar0 = 1 + half * kMidBars, bar_half = bar0 + kMidBars - 1;

@@ -425,3 +425,24 @@ def test_pinned_results_on_the_edge_cases(lib, oracle_mod, ref_synthetic):
     for mode in (abea.MODE_PLAIN, abea.MODE_BATCHED):
         gp, gc = _pinned_call(abea.Context(0, mode), batch)
         assert_same_alignments(batch, gp, gc, op, oc)
+
+
+@pytest.mark.parametrize("workload", ["f5c_batch", "reads1024"])
+def test_more_wide_reads_than_blocks(lib, workload):
+    """Every read on the wide shape: the blocks pull wide reads one after another
+    (each reusing its traceback scratch slot), so most blocks fill several.  The
+    AlignedPairs and best scores equal the plain form's."""
+    from abea_gb300 import synth
+    batch = synth.make_batch(workload, seed=3)
+    ctx = abea.Context(0, abea.MODE_BATCHED)
+    ctx.set_option(abea.OPT_LONG_READ_BANDS, 1)
+    dev = ctx.upload(batch)
+    dev.run()
+    gp, gc = dev.results()
+    gb = dev.best_scores()
+    pctx = abea.Context(0, abea.MODE_PLAIN)
+    pdev = pctx.upload(batch)
+    pdev.run()
+    pp, pc = pdev.results()
+    assert_same_alignments(batch, gp, gc, pp, pc)
+    assert np.array_equal(gb.view(np.uint32), pdev.best_scores().view(np.uint32))

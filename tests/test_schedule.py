@@ -21,22 +21,29 @@ def wide_threshold(bands, blocks=152):
 
 def n_wide(bands, blocks=152):
     thr = wide_threshold(bands, blocks)
-    return 0 if thr >= 2**62 else int(min(np.sum(np.asarray(bands) >= thr), blocks))
+    return 0 if thr >= 2**62 else int(np.sum(np.asarray(bands) >= thr))
 
 
-def test_one_long_read_among_short_ones_goes_wide():
-    """The f5c batch shape: its longest reads bound the batch on the warp shape."""
+def test_latency_bound_batch_goes_all_wide():
+    """The f5c batch shape: its longest read bounds the batch whatever the split,
+    and with every read on the wide shape (the blocks pulling them longest first)
+    nothing else is longer (measured 8.46 ms, against 8.49-9.10 ms for the best
+    one-wide-read-per-block split and 36.1 ms with none)."""
     from abea_gb300 import synth
     nb = synth.make_batch("f5c_batch", seed=1).n_bands()
-    k = n_wide(nb)
-    assert 60 <= k <= 130, k   # measured best: 80-100 wide reads (10.19 ms; 11.57 with 50, 39.2 with none)
+    assert n_wide(nb) == len(nb)
 
 
-def test_flat_length_distribution_stays_on_the_warp_shape():
-    """1,024 reads of 1-10 kb: wide reads would take whole SMs for little gain
-    (measured 24.4 ms with none, 44.6 ms with one per block)."""
+def test_few_reads_per_sm_go_all_wide_many_stay_on_the_warp_shape():
+    """1,024 reads of 1-10 kb (about 7 per SM): every read wide, 18.5 ms against
+    20.8 ms with none.  4,096 such reads (27 per SM): none, 35.5 ms against 68.5
+    with every read wide, because 16 warp-shape reads per SM issue more per SM
+    than one wide read."""
     rng = np.random.default_rng(11)
     lens = rng.integers(1000, 10001, 1024)
+    nb = lens - 5 + (lens * 1.71).astype(np.int64) + 2
+    assert n_wide(nb) == 1024
+    lens = rng.integers(1000, 10001, 4096)
     nb = lens - 5 + (lens * 1.71).astype(np.int64) + 2
     assert n_wide(nb) == 0
     assert n_wide(np.full(4096, 27000)) == 0
