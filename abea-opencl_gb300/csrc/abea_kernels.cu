@@ -822,27 +822,27 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const float l = exact_skip(left, cc.skip_h, cc.skip_l, okl);
             float best = pick_l(best_du, from_du, l, from);
             const bool bad = valid && !(okd && oku && okl);
+            best = valid ? best : -INFINITY;
+            from = valid ? from : 0u;
+            const bool here = !kMid && (t == 127) && (k0 <= -1) && (k0 >= -kBand);
+            best = here ? tv : best;
+            from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
+            ws.sc[b & 1][t] = best;  // stored before the check: only the rare path stores again
             if (__any_sync(kFull, bad)) {
                 // Rare: a proof failed in some lane, whose cell takes the reference's
-                // FP64 arithmetic.  The whole warp calls (a divergent branch around
-                // the call cost 20 cycles per band); the other lanes pass k-mer 0
-                // and event 0 of the read, which exist because the bad lane's cell
-                // does, and drop the result.
+                // FP64 arithmetic and stores its score again.  The whole warp calls (a
+                // divergent branch around the call cost 20 cycles per band); the other
+                // lanes pass k-mer 0 and event 0 of the read, which exist because the
+                // bad lane's cell does, and drop the result.
                 const int64_t ko = r.km_off + (bad ? k0 + o : 0);
                 const SlowCell c = slow_cell_call(lp, s1, left, a.ev_mean[r.ev_off + (bad ? e0 - o : 0)], a.km_gm[ko],
                                                   a.km_sd[ko], a.km_k1[ko], cc.lp_step, cc.lp_stay, cc.lp_skip);
-                best = bad ? c.best : best;
-                from = bad ? c.from : from;
-                slow += bad ? 1 : 0;
+                const bool use = bad && !here;
+                best = use ? c.best : best;
+                from = use ? c.from : from;
+                slow += use ? 1 : 0;
+                ws.sc[b & 1][t] = best;
             }
-            best = valid ? best : -INFINITY;
-            from = valid ? from : 0u;
-            if (!kMid) {
-                const bool here = (t == 127) && (k0 <= -1) && (k0 >= -kBand);
-                best = here ? tv : best;
-                from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
-            }
-            ws.sc[b & 1][t] = best;
             if (q == kWideChunk - 1 && j + kRing < n_chunks)
                 named_bar_arrive(kBarEmpty + s, kPair);  // chunk j read: E may refill its slot
             lp = left;
