@@ -629,6 +629,16 @@ __device__ __forceinline__ void named_bar_sync(int id, int n) {
 __device__ __forceinline__ void named_bar_arrive(int id, int n) {
     asm volatile("bar.arrive %0, %1;\n" ::"r"(id), "r"(n) : "memory");
 }
+// bar.sync that also returns whether p held in any of the n threads
+__device__ __forceinline__ bool named_bar_any(int id, int n, bool p) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, %2, %3, pi;\n selp.u32 %0, 1, 0, po;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)p), "r"(id), "r"(n)
+        : "memory");
+    return r != 0u;
+}
 
 __device__ __forceinline__ bool band_moves_right(float ll, float ur, int b) {
     // Suzuki-Kasahara (GPU/align_cuda.cl:394-430); both ends -inf: alternate
@@ -782,15 +792,24 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     // column (and neither does band bb-1, whose bookkeeping the chunk finishes): k0
     // and e0 each move by at most one per band, so the placement of band bb-1
     // decides it for the whole chunk.
-    auto chunk = [&](int j, auto last, auto mid) {
+    // kOpt: optimistic (middle chunks only): no per-band check of the exactness
+    // proofs; each thread ORs its failed proofs into `dirty`, the barrier that ends
+    // the chunk reduces them (open_chunk), and a chunk with any is done again with
+    // the checks (kRedo: its emissions are still in the ring, whose slot is
+    // released only after that barrier).  The chunk's first chain barrier is the
+    // caller's (open_chunk), except in a redo.
+    bool dirty = false;
+    auto chunk = [&](int j, auto last, auto mid, auto opt, auto redo) {
         constexpr bool kLast = decltype(last)::value, kMid = decltype(mid)::value;
+        constexpr bool kOpt = decltype(opt)::value, kRedo = decltype(redo)::value;
+        static_assert(!kOpt || kMid, "only middle chunks run optimistic");
         const int s = j % kRing, bb = 2 + kWideChunk * j;
 #pragma unroll
         for (int q = 0; q < kWideChunk; ++q) {
             const int b = bb + q;
             if (kLast && b >= n_bands) break;
-            named_bar_sync(kBarChain, kSlots);                   // band b-1's scores are in shared memory
-            if (q == 0) named_bar_sync(kBarFull + s, kPair);     // chunk j's emissions are in the ring
+            if (q > 0 || kRedo) named_bar_sync(kBarChain, kSlots);  // band b-1's scores are in shared memory
+            if (q == 0 && !kRedo) named_bar_sync(kBarFull + s, kPair);  // chunk j's emissions are in the ring
             const int pb = (b - 1) & 1;
             const float ll = ws.sc[pb][k0 & 127];
             const float ur = ws.sc[pb][(k0 + kBand - 1) & 127];
@@ -828,7 +847,9 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             best = here ? tv : best;
             from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
             ws.sc[b & 1][t] = best;  // stored before the check: only the rare path stores again
-            if (__any_sync(kFull, bad)) {
+            if (kOpt) {
+                dirty = dirty || bad;
+            } else if (__any_sync(kFull, bad)) {
                 // Rare: a proof failed in some lane, whose cell takes the reference's
                 // FP64 arithmetic and stores its score again.  The whole warp calls (a
                 // divergent branch around the call cost 20 cycles per band); the other
@@ -843,7 +864,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
                 slow += use ? 1 : 0;
                 ws.sc[b & 1][t] = best;
             }
-            if (q == kWideChunk - 1 && j + kRing < n_chunks)
+            if (!kOpt && !kRedo && q == kWideChunk - 1 && j + kRing < n_chunks)
                 named_bar_arrive(kBarEmpty + s, kPair);  // chunk j read: E may refill its slot
             lp = left;
             s1 = best;
@@ -854,14 +875,63 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             hip = hi;
         }
     };
+    // The state an optimistic chunk starts from (band bb-1's placement, score,
+    // backpointer and the diagonal of band bb, the backpointer word, the band
+    // origins: its last band may have started the next 32), for its redo.
+    int sv_k0 = 0, sv_e0 = 0, sv_myk0 = 0, pj = -1;
+    float sv_s1 = 0.f, sv_lp = 0.f;
+    uint32_t sv_from = 0u, sv_tw = 0u;
+    using F = std::false_type;
+    using T = std::true_type;
+    // The barrier that ends band bb-1 before chunk j (bb = 2 + 4j), or before the
+    // last band's bookkeeping (j = n_chunks).  After an optimistic chunk it also
+    // reduces that chunk's failed proofs; with any, the chunk is done again from
+    // its saved state, with the checks.  Then the chunk's ring slot is released.
+    auto open_chunk = [&](int j) {
+        if (pj < 0) {
+            named_bar_sync(kBarChain, kSlots);
+            return;
+        }
+        if (named_bar_any(kBarChain, kSlots, dirty)) {
+            k0 = k0p = sv_k0;
+            e0 = e0p = sv_e0;
+            s1 = sv_s1;
+            lp = sv_lp;
+            from_p = sv_from;
+            tw = sv_tw;
+            my_k0 = sv_myk0;
+            ws.sc[(1 + kWideChunk * pj) & 1][t] = s1;  // band bb-1's scores, which the chunk overwrote
+            chunk(pj, F{}, T{}, F{}, T{});              // its first barrier publishes them
+            named_bar_sync(kBarChain, kSlots);
+        }
+        if (pj + kRing < n_chunks) named_bar_arrive(kBarEmpty + pj % kRing, kPair);  // E may refill the slot
+        pj = -1;
+        dirty = false;
+        (void)j;
+    };
     const int n_full = (n_bands - 2) / kWideChunk;
     for (int j = 0; j < n_full; ++j) {
-        if (k0 >= 0 && k0 + kWideChunk <= n_kmers - 1 - kBand && e0 >= kBand - 1 && e0 + kWideChunk <= n_events - 1)
-            chunk(j, std::false_type{}, std::true_type{});
-        else
-            chunk(j, std::false_type{}, std::false_type{});
+        open_chunk(j);
+        if (k0 >= 0 && k0 + kWideChunk <= n_kmers - 1 - kBand && e0 >= kBand - 1 && e0 + kWideChunk <= n_events - 1) {
+            sv_k0 = k0;
+            sv_e0 = e0;
+            sv_s1 = s1;
+            sv_lp = lp;
+            sv_from = from_p;
+            sv_tw = tw;
+            sv_myk0 = my_k0;
+            pj = j;
+            chunk(j, F{}, T{}, T{}, F{});
+        } else {
+            chunk(j, F{}, F{}, F{}, F{});
+        }
     }
-    if (n_full < n_chunks) chunk(n_full, std::true_type{}, std::false_type{});
+    if (n_full < n_chunks) {
+        open_chunk(n_full);
+        chunk(n_full, T{}, F{}, F{}, F{});
+    } else if (n_bands > 2) {
+        open_chunk(n_chunks);  // the last chunk may have been optimistic
+    }
     if (n_bands > 2) {  // the last band's bookkeeping and the stores it closes
         const int bl = n_bands - 1;
         book(bl, -1, true);
