@@ -543,12 +543,14 @@ static abea_status_t ensure_device(abea_batch* b, bool scores, size_t reserve = 
 }
 
 // Copies a batch to the device.  bases_events = false leaves out the bases and
-// the events (the pre stage then reads them from the caller's pinned memory).
-static abea_status_t upload(abea_batch* b, const HostInputs& in, cudaStream_t st, bool bases_events = true) {
+// the events (the pre stage then reads them from the caller's pinned memory);
+// reads_pinned, when given, is a pinned copy of the read descriptors to copy from.
+static abea_status_t upload(abea_batch* b, const HostInputs& in, cudaStream_t st, bool bases_events = true,
+                            const ReadDesc* reads_pinned = nullptr) {
     if (b->n_reads == 0) return ABEA_OK;
     CUDA_TRY(cudaMemsetAsync(b->d_aux, 0, kAuxBytes, st));  // no input or output mirror
-    CUDA_TRY(cudaMemcpyAsync(b->d_reads, b->reads.data(), sizeof(ReadDesc) * b->reads.size(),
-                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(b->d_reads, reads_pinned ? reads_pinned : b->reads.data(),
+                             sizeof(ReadDesc) * b->reads.size(), cudaMemcpyHostToDevice, st));
     if (bases_events && b->seq_bytes > 0)
         CUDA_TRY(cudaMemcpyAsync(b->d_seq, in.read, (size_t)b->seq_bytes, cudaMemcpyHostToDevice, st));
     if (bases_events && b->n_events_total > 0)
@@ -1357,8 +1359,11 @@ static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_al
     }
     const bool mirror = im.seq || om.pairs || om.n_pairs;
     // pinned: the mirrors as copied to the device, then the batch's counters and
-    // statuses as copied back (read before the call returns, after one synchronize)
-    const size_t aux_bytes = kAuxBytes + sizeof(unsigned long long) * 4 + sizeof(int32_t) * (size_t)b->n_reads;
+    // statuses as copied back (read before the call returns, after one synchronize),
+    // then the read descriptors as copied to the device
+    const size_t desc_at = (kAuxBytes + sizeof(unsigned long long) * 4 + sizeof(int32_t) * (size_t)b->n_reads + 15) &
+                           ~(size_t)15;
+    const size_t aux_bytes = desc_at + sizeof(ReadDesc) * (size_t)b->n_reads;
     if (c->h_aux_bytes < aux_bytes) {
         if (c->h_aux) cudaFreeHost(c->h_aux);
         c->h_aux = nullptr;
@@ -1370,8 +1375,32 @@ static abea_status_t align_batch_impl(abea_ctx* c, const HostInputs& in, abea_al
         }
         c->h_aux_bytes = aux_bytes;
     }
+    if (im.seq && c->mode == ABEA_MODE_BATCHED && c->wide_cluster == 0) {
+        // The first reads the kernel starts are copied to HBM before it (up to 4
+        // reads, 1.5 MB): otherwise they share the CPU-GPU link with every other
+        // read's first loads, and the first is the longest.
+        prepare_order(c, b);
+        int64_t bytes = 0;
+        for (size_t q = 0; q < b->dev_order.size() && q < 4; ++q) {
+            ReadDesc& r = b->reads[(size_t)b->dev_order[q]];
+            const int64_t rb = (int64_t)r.n_kmers + ABEA_KMER_SIZE - 1 + (int64_t)sizeof(abea_event_t) * r.n_events;
+            if (r.skip || bytes + rb > ((int64_t)3 << 19)) break;
+            r.in_hbm = 1;
+            bytes += rb;
+        }
+    }
+    ReadDesc* desc = (ReadDesc*)(c->h_aux + desc_at);
+    if (b->n_reads > 0) memcpy(desc, b->reads.data(), sizeof(ReadDesc) * (size_t)b->n_reads);
     CUDA_TRY(cudaEventRecord(c->ev[4], c->stream));
-    if ((st = upload(b, in, c->stream, im.seq == nullptr))) return st;
+    if ((st = upload(b, in, c->stream, im.seq == nullptr, desc))) return st;
+    if (im.seq)
+        for (const ReadDesc& r : b->reads) {
+            if (!r.in_hbm) continue;
+            CUDA_TRY(cudaMemcpyAsync(b->d_seq + r.seq_off, in.read + r.seq_off,
+                                     (size_t)r.n_kmers + ABEA_KMER_SIZE - 1, cudaMemcpyHostToDevice, c->stream));
+            CUDA_TRY(cudaMemcpyAsync(b->d_ev + r.ev_src, in.event_table + r.ev_src,
+                                     sizeof(abea_event_t) * (size_t)r.n_events, cudaMemcpyHostToDevice, c->stream));
+        }
     if (mirror) {
         memset(c->h_aux, 0, kAuxBytes);
         memcpy(c->h_aux, &im, sizeof(im));

@@ -56,6 +56,8 @@ struct ReadDesc {
     float stay_h, stay_l;
     float scale, shift, var, log_var;
     int32_t skip;       // 1: nothing to align (n_kmers <= 0 or n_events <= 0)
+    int32_t in_hbm;     // 1: the pre stage reads this read's bases and events from HBM even
+                        // when the batch's inputs are read from host memory
 };
 
 // Band-score checkpoints of reads whose trace exceeds the memory budget: at

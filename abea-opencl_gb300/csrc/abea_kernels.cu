@@ -96,7 +96,8 @@ __device__ __forceinline__ CellConsts make_consts(const ReadDesc& r, const Globa
 //
 // The bases and events come from HBM, or, when the caller's buffers are pinned
 // (a.inm), straight from host memory over the CPU-GPU link: no copy of the
-// inputs precedes the kernel, and every read's pre stage loads its own.  A thread
+// inputs precedes the kernel, and every read's pre stage loads its own (but the
+// first few reads the kernel starts, copied to HBM before it: in_hbm).  A thread
 // takes kPreUnroll k-mer positions (kEvUnroll events) per pass with every load
 // issued before any use (indexes clamped into the read), so that many round trips
 // to host memory are in flight at once: a warp-shape read's pre stage is latency-
@@ -105,7 +106,7 @@ constexpr int kPreUnroll = 4, kEvUnroll = 16;
 __device__ __forceinline__ void pre_read(const PreArgs& a, int i, int t, int nt) {
     const ReadDesc r = a.reads[i];
     if (r.skip) return;
-    const InMirror* m = a.inm;
+    const InMirror* m = r.in_hbm ? nullptr : a.inm;
     const char* seq = a.seq;
     const abea_event_t* ev_in = a.ev_in;
     if (m) {
