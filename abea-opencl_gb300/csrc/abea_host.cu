@@ -586,8 +586,12 @@ static int64_t d2h_bytes(const abea_batch* b) {
 // Then every read on the wide shape, the blocks pulling them longest first: the
 // longest read at kWideCyc per band, or all the bands over the blocks at
 // kWideSmCyc per band per block.  That wins when it is within 2% of the first
-// (it cannot be shorter than the longest read, which bounds both), except with
-// checkpointed reads, which run on the warp shape and would start last.
+// (it cannot be shorter than the longest read, which bounds both) and either the
+// longest read bounds it or there are at most 8 reads per block (with more, the
+// warp shape's 16 warps per SM hide each other's latency better than the first
+// estimate assumes: the serving stream's batches of ~4,000 reads of median 8 kb
+// took 1.23 s every read wide against 0.99 s split), except with checkpointed
+// reads, which run on the warp shape and would start last.
 // Calibrated on GB300 by sweeping the number of wide reads: the f5c batch and the
 // 1,024-read batch of 1-10 kb reads are fastest with every read wide (8.46 and
 // 18.5 ms, against 8.49-9.10 and 20.8 at the best one-per-block split); the
@@ -642,8 +646,12 @@ static int64_t heuristic_threshold(const abea_batch* b, int blocks) {
         }
     }
     if (!any_ck && !wide_ok.empty()) {
-        const double t_all = std::max((double)wide_ok[0] * kWideCyc, all_bands * kWideSmCyc / std::max(blocks, 1));
-        if (t_all <= best_t * 1.02) return 1;
+        const double t_lat = (double)wide_ok[0] * kWideCyc, t_thr = all_bands * kWideSmCyc / std::max(blocks, 1);
+        // at more than 8 reads per block the warp shape's warps hide each other's
+        // latency and the split's estimate above is too long: every read wide only
+        // where the longest read bounds it anyway, or with few reads per block
+        const bool few = (double)n <= 8.0 * blocks;
+        if ((t_thr <= t_lat || few) && std::max(t_lat, t_thr) <= best_t * 1.02) return 1;
     }
     return best_n > 0 ? wide_ok[(size_t)best_n - 1] : INT64_MAX;
 }
