@@ -428,10 +428,12 @@ static abea_status_t plan(abea_batch* b, const HostInputs& in, int var_aware, in
     int32_t n_spec = 0;
     for (const ReadDesc& r : b->reads)
         if (!r.skip && !r.ck && r.n_bands >= kSpecMinBands) ++n_spec;
-    // one scratch slot per block of the batched kernel (a block walks one wide read at a time)
+    // one scratch slot per block that starts on a wide read (a block walks one wide read
+    // at a time and keeps its slot; the first picks take the longest reads, so at most
+    // one slot per qualifying read)
     const int grid = b->ctx ? std::max(batched_blocks_per_sm(false), batched_blocks_per_sm(true)) * b->ctx->sm_count
                             : kSpecMaxSlots;
-    b->n_spec = n_spec > 0 ? std::min(std::max(grid, 1), kSpecMaxSlots) : 0;
+    b->n_spec = std::min(std::min(n_spec, std::max(grid, 1)), kSpecMaxSlots);
     b->pair_cap = 2 * ev_end;
     b->band_cells = cells;
     // longest first; ties by index

@@ -1768,7 +1768,8 @@ struct WidePostSmem {  // overlays the wide fill's shared memory once the fill i
 };
 
 // All kWideThreads threads of the block call it.
-__device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* wide_mem, Rings& rg0, int t) {
+__device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, uint8_t* wide_mem, Rings& rg0, int t,
+                                int slot_of_block) {
     const int warp = t >> 5, lane = t & 31;
     WidePostSmem& ps = *reinterpret_cast<WidePostSmem*>(wide_mem);
     const ReadDesc r = a.reads[ri];
@@ -1815,7 +1816,7 @@ __device__ void post_wide_block(const CoreArgs& ca, const PostArgs& a, int ri, u
                 }
             ps.best = b;
             ps.best_e = b > -INFINITY ? be : 0;
-            ps.slot = blockIdx.x;  // the block's scratch slot for the maps (one wide read at a time)
+            ps.slot = slot_of_block;  // the block's scratch slot for the maps (one wide read at a time)
         }
     }
     __syncthreads();
@@ -2072,6 +2073,7 @@ struct BatchedSmem {
     // warps' entries (post[8 * half] on), which no other warp touches meanwhile
     PostSmem post[kBatchedWarps];
     int32_t pick;                      // the block's wide read, or -1
+    int32_t wide_slot;                 // the block's first pick: its traceback scratch slot
     int32_t free_rank;                 // rank among the blocks with neither a wide nor medium reads, or -1
     int32_t mid_block;                 // 1: a block of the medium reads
     int32_t mid_pick[2];               // each half's medium read
@@ -2104,12 +2106,14 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
     if (t == 0) {
         const int q = atomicAdd(&a.queue[0], 1);
         sm.pick = q < a.n_wide ? a.order[q] : -1;
+        sm.wide_slot = q;  // the block's traceback scratch slot: wide reads go longest first, so only
+                           // the first blocks' reads (and the reads they pull later) need one
         sm.mid_block = (q >= a.n_wide && q < a.n_wide + n_midb) ? 1 : 0;
         sm.free_rank = q < a.n_wide + n_midb ? -1 : q - a.n_wide - n_midb;
     }
     __syncthreads();
     int wide_read = sm.pick;
-    const int free_rank = sm.free_rank;
+    const int free_rank = sm.free_rank, wide_slot = sm.wide_slot;
     while (wide_read >= 0) {
         const ReadDesc& r = a.reads[wide_read];
         pre_read(pa, wide_read, t, kWideThreads);
@@ -2118,7 +2122,7 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
         __syncthreads();
         __threadfence_block();
         // the whole block walks the wide read's traceback (the fill's shared memory is free)
-        post_wide_block(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0], t);
+        post_wide_block(a, p, wide_read, reinterpret_cast<uint8_t*>(&sm.wide), sm.warp_rings[0], t, wide_slot);
         // then the next wide read past the first wave (one per block), longest first
         __syncthreads();  // the traceback is done with the block's shared memory and the pick
         if (t == 0) {

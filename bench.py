@@ -573,8 +573,9 @@ def align_threads_report(pkg, batch, threads: int = 8, max_reads: int = 256):
             "band_cells_per_s": cells / dt, "identical_to_batched": bool(same),
             "per_thread_device_footprint": "one context per calling thread (a stream, 24 CUDA events) and a "
                                            "device slab grown to that thread's largest read so far: about 132 B "
-                                           "per band + 48 B per event + 17 B per base, plus 136 KB fixed "
-                                           "(a 20 kb read: ~9 MB)"}
+                                           "per band + 48 B per event + 17 B per base, plus 136 KB fixed, plus "
+                                           "512 KB of traceback scratch for a read of 512 bands or more "
+                                           "(a 20 kb read: ~9.5 MB)"}
 
 
 def ours(args, dist):

@@ -178,8 +178,8 @@ const char *abea_version(void);
  * calling thread gets its own context (a stream and 24 CUDA events) on the
  * current device, created by its first call and destroyed when the thread
  * exits, and a device slab grown to that thread's largest read so far (about
- * 132 bytes per band + 48 per event + 17 per base, plus 136 KB; a 20 kb read:
- * about 9 MB).  Each read runs alone on the wide shape of the batched form. */
+ * 132 bytes per band + 48 per event + 17 per base, plus 136 KB, plus 512 KB of
+ * traceback scratch for a read of 512 bands or more; a 20 kb read: about 9.5 MB).  Each read runs alone on the wide shape of the batched form. */
 int32_t abea_align(abea_aligned_pair_t *out_2, char *sequence, int32_t sequence_len,
                    abea_event_table_t events, abea_model_t *models, abea_scalings_t scaling,
                    float sample_rate);
