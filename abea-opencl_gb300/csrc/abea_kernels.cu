@@ -8,26 +8,27 @@
 //   post  (post_read_warp)     best end, traceback, reverse, quality checks.
 //                              Replaces align_kernel_post (GPU/align_cuda.cl:618-899).
 //
-// Fill shapes (both bit-exact, same trace layout):
-//   warp — one warp per read, lane l holds k-mer slots 4l..4l+3.  Neighbour
-//          scores move by one shuffle per band, the band move is decided from two
-//          shuffled end cells; no block barrier.  Most work per SM.
-//   wide — sixteen warps per read in four groups of 128 threads (one slot per
-//          thread each): one group runs only the band-to-band chain, the others
-//          prepare emissions, diagonal candidates and bookkeeping ahead of it;
-//          cells exchanged in shared memory with one barrier per band.  Shortest
-//          band latency: used for the longest reads of a batch.
+// Fill shapes (all bit-exact, same trace layout):
+//   warp   — one warp per read, lane l holds k-mer slots 4l..4l+3.  Neighbour
+//            scores move by one shuffle per band, the band move is decided from two
+//            shuffled end cells; no block barrier.  Most reads per SM.
+//   wide   — twelve warps of a 512-thread block per read (fill_chain): four run
+//            the band-to-band chain (one slot per thread, one barrier per band, cells
+//            exchanged in shared memory), eight compute the emissions and their exact
+//            splits up to 16 bands ahead into a ring.  Shortest band latency.
+//   medium — the same chain and producer with four producer warps, two reads per
+//            block (off unless tuned).
 // Forms:
 //   plain   — pre, core (warp shape, one block per read), post (one block per
 //             read): the reference's three launches.
 //   batched — one persistent kernel of one block per SM (each read's pre runs
-//             in the block or warp that fills it): each block
-//             first takes one of the longest reads on the wide shape and walks its
-//             traceback with the whole block (post_wide_block); the blocks without a
-//             wide read take the first wave of the other reads round-robin, one per
-//             warp, and then every warp pulls the rest longest-first from a device
-//             queue; a warp-shape read's post runs in the warp that filled it, right
-//             after its fill (trace still in L2).
+//             in the block or warp that fills it): the blocks take the wide reads
+//             from a queue, longest first, one after another, each walking its
+//             read's traceback with the whole block (post_wide_block); then the
+//             medium reads; the blocks without a wide read take the first wave of the
+//             other reads round-robin, one per warp, and then every warp pulls the
+//             rest longest-first from a device queue; a warp-shape read's post runs
+//             in the warp that filled it, right after its fill (trace still in L2).
 //   The wide shape on a cluster of two blocks (emissions on the second SM) is an
 //   option, measured slower.
 #include <cooperative_groups.h>
@@ -2098,10 +2099,12 @@ __global__ void __launch_bounds__(kWideThreads, 1) abea_batched_kernel(CoreArgs 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchedSmem& sm = *reinterpret_cast<BatchedSmem*>(smem_raw);
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    // phase 1: one of the longest reads on the wide shape
-    // The first blocks to arrive take the wide reads, one each; the next ones the
-    // medium reads (two at a time per block, enough blocks for each half to start
-    // one); the others the first wave of the warp-shape reads.
+    // phase 1: the wide reads, longest first
+    // Each block's first pick decides its role: the first blocks to arrive take a
+    // wide read each (and then pull the wide reads past the first wave, one after
+    // another); the next ones the medium reads (two at a time per block, enough
+    // blocks for each half to start one); the others the first wave of the
+    // warp-shape reads.
     const int n_midb = min((a.n_mid + 1) / 2, max((int)gridDim.x - a.n_wide, 0));
     if (t == 0) {
         const int q = atomicAdd(&a.queue[0], 1);
