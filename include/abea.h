@@ -115,9 +115,11 @@ typedef enum {
  *            512-thread block per SM: the longest reads on the wide shape
  *            (twelve warps: four run the band-to-band chain, eight compute the
  *            emissions ahead of it; the traceback is walked by the whole block),
- *            the rest one warp each, first spread round-robin over the blocks,
- *            then pulled longest-first from a device queue; replayed as one CUDA
- *            graph. */
+ *            which the blocks pull longest first, one after another (every read,
+ *            when the batch's longest read bounds it or it has few reads per SM);
+ *            the rest one warp each, first spread round-robin over the other
+ *            blocks, then pulled longest-first from a device queue; replayed as
+ *            one CUDA graph. */
 typedef enum { ABEA_MODE_PLAIN = 0, ABEA_MODE_BATCHED = 1 } abea_mode_t;
 
 /* Context options (abea_ctx_set_option). */
