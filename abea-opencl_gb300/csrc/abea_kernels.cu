@@ -766,10 +766,14 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     // last-column store cost 27 cycles per band).  The placement of every fourth
     // band (the one E reads) goes to the ring k0h; band origins are kept one per
     // lane of warp 0 and stored 32 bands at a time.
-    auto book = [&](int bk, int q1, bool last_col) {
-        const int qq = q1 >= 0 ? q1 : (bk & 3);
-        tw |= from_p << (8 * qq);
-        my_k0 = ((bk & 31) == lane) ? k0p : my_k0;
+    auto book = [&](int bk, int q1, bool last_col, bool mine) {
+        if (q1 >= 0) {  // the byte's place known when compiled: one byte insert
+            constexpr unsigned kSel[4] = {0x3214u, 0x3240u, 0x3410u, 0x4210u};
+            tw = __byte_perm(tw, from_p, kSel[q1 & 3]);
+        } else {
+            tw |= from_p << (8 * (bk & 3));
+        }
+        my_k0 = mine ? k0p : my_k0;
         if (t == 0 && (bk & 3) == 0) ws.k0h[bk & 63] = k0p;
         if (last_col) {
             const int ol = n_kmers - 1 - k0p;
@@ -806,6 +810,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
         constexpr bool kOpt = decltype(opt)::value, kRedo = decltype(redo)::value;
         static_assert(!kOpt || kMid, "only middle chunks run optimistic");
         const int s = j % kRing, bb = 2 + kWideChunk * j;
+        const int dl = (lane - 1 - kWideChunk * j) & 31;  // band bb-1+q's origin goes to lane (bb-1+q) & 31: dl == q
 #pragma unroll
         for (int q = 0; q < kWideChunk; ++q) {
             const int b = bb + q;
@@ -820,7 +825,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const float2 mm = ws.emm[s][q][t];
             const float tv = ws.trim[s][q];
             // band b-1's bookkeeping (bands 2 + 4j + q - 1: b-1 & 3 == (q + 1) & 3)
-            book(b - 1, (q + 1) & 3, !kMid);
+            book(b - 1, (q + 1) & 3, !kMid, dl == q);
             if (q == 2) {  // band b-1 closes a tile of four bands, every eighth one 32 bands
                 store_tile(b - 1);
                 store_origins(b - 1, ((b - 1) & 31) == 31);
@@ -845,7 +850,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const bool proven = okd && oku && okl;
             const bool bad = valid && !proven;
             best = valid ? best : -INFINITY;
-            from = valid ? from : 0u;
+            if (!kMid) from = valid ? from : 0u;  // a middle chunk's invalid slots are outside the band
             const bool here = !kMid && (t == 127) && (k0 <= -1) && (k0 >= -kBand);
             best = here ? tv : best;
             from = here ? (tv == -INFINITY ? 0u : ABEA_FROM_U) : from;
@@ -939,7 +944,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     }
     if (n_bands > 2) {  // the last band's bookkeeping and the stores it closes
         const int bl = n_bands - 1;
-        book(bl, -1, true);
+        book(bl, -1, true, (bl & 31) == lane);
         store_tile(bl);
         store_origins(bl, true);
     }
