@@ -747,7 +747,9 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     float* scores = kScores ? a.scores + r.band_off * kSlots : nullptr;
     const int sl_last = (n_kmers - 1) & (kSlots - 1);
 
-    int k0 = -1 - kBand / 2, e0 = kBand / 2;         // band 1 (band 0 is (49,-51), band 1 moved down)
+    // band b's placement: lower-left k-mer k0, event e0 = b - 2 - k0 (a band's cells
+    // lie on one anti-diagonal), so only k0 is carried
+    int k0 = -1 - kBand / 2;                         // band 1 (band 0 is (49,-51), band 1 moved down)
     float s1 = (t == 127) ? a.g.trim_f : -INFINITY;  // band b-1's score of this slot
     float lp = (t == 0) ? 0.0f : -INFINITY;          // band b-2's score of slot t-1: band b's diagonal
     ws.sc[1][t] = s1;
@@ -758,7 +760,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     int my_k0 = k0;                                      // band origins: band b in lane b & 31 (bands 0, 1: -51)
     uint32_t tw = 0u;                                    // backpointers of bands 4m..4m+3, byte b & 3
     uint32_t from_p = (t == 127) ? ABEA_FROM_U : 0u;     // band b-1's backpointer (band 1: the trim cell)
-    int k0p = k0, e0p = e0, lop = 0, hip = 0;            // band b-1's placement and computed offsets
+    int k0p = k0, lop = 0, hip = 0;                      // band b-1's placement and computed offsets
     unsigned long long slow = 0;
     // Band bk's bookkeeping; q1 = bk & 3 when known at compile time, else -1.  No
     // branches: a branch in the unrolled band body splits the code the compiler
@@ -777,6 +779,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
         if (t == 0 && (bk & 3) == 0) ws.k0h[bk & 63] = k0p;
         if (last_col) {
             const int ol = n_kmers - 1 - k0p;
+            const int e0p = bk - 2 - k0p;
             if (t == sl_last && ol >= lop && ol < hip && in_bounds(e0p - ol, n_events, a.counters))
                 lastc[e0p - ol] = s1;
         }
@@ -836,7 +839,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             const float u = exact_from_split(s1, EmSplit{ep.y, ep.w}, mm.y, oku);
             const bool right = band_moves_right(ll, ur, b);
             k0 += right ? 1 : 0;
-            e0 += right ? 0 : 1;
+            const int e0 = b - 2 - k0;
             int lo = 0, hi = kBand;
             if (!kMid) band_range(k0, e0, n_events, n_kmers, lo, hi);
             const int o = (t - k0) & 127;
@@ -880,7 +883,6 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             s1 = best;
             from_p = from;
             k0p = k0;
-            e0p = e0;
             lop = lo;
             hip = hi;
         }
@@ -888,7 +890,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     // The state an optimistic chunk starts from (band bb-1's placement, score,
     // backpointer and the diagonal of band bb, the backpointer word, the band
     // origins: its last band may have started the next 32), for its redo.
-    int sv_k0 = 0, sv_e0 = 0, sv_myk0 = 0, pj = -1;
+    int sv_k0 = 0, sv_myk0 = 0, pj = -1;
     float sv_s1 = 0.f, sv_lp = 0.f;
     uint32_t sv_from = 0u, sv_tw = 0u;
     using F = std::false_type;
@@ -904,7 +906,6 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
         }
         if (named_bar_any(kBarChain, kSlots, dirty)) {
             k0 = k0p = sv_k0;
-            e0 = e0p = sv_e0;
             s1 = sv_s1;
             lp = sv_lp;
             from_p = sv_from;
@@ -922,9 +923,9 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     const int n_full = (n_bands - 2) / kWideChunk;
     for (int j = 0; j < n_full; ++j) {
         open_chunk(j);
+        const int e0 = kWideChunk * j - 1 - k0;  // band bb-1's event (bb = 2 + 4j)
         if (k0 >= 0 && k0 + kWideChunk <= n_kmers - 1 - kBand && e0 >= kBand - 1 && e0 + kWideChunk <= n_events - 1) {
             sv_k0 = k0;
-            sv_e0 = e0;
             sv_s1 = s1;
             sv_lp = lp;
             sv_from = from_p;
