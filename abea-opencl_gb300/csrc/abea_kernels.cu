@@ -760,7 +760,6 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
     int my_k0 = k0;                                      // band origins: band b in lane b & 31 (bands 0, 1: -51)
     uint32_t tw = 0u;                                    // backpointers of bands 4m..4m+3, byte b & 3
     uint32_t from_p = (t == 127) ? ABEA_FROM_U : 0u;     // band b-1's backpointer (band 1: the trim cell)
-    int k0p = k0, lop = 0, hip = 0;                      // band b-1's placement and computed offsets
     unsigned long long slow = 0;
     // Band bk's bookkeeping; q1 = bk & 3 when known at compile time, else -1.  No
     // branches: a branch in the unrolled band body splits the code the compiler
@@ -775,11 +774,13 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
         } else {
             tw |= from_p << (8 * (bk & 3));
         }
-        my_k0 = mine ? k0p : my_k0;
-        if (t == 0 && (bk & 3) == 0) ws.k0h[bk & 63] = k0p;
+        // band bk's placement is still k0: the band after it moves k0 after this
+        my_k0 = mine ? k0 : my_k0;
+        if (t == 0 && (bk & 3) == 0) ws.k0h[bk & 63] = k0;
         if (last_col) {
-            const int ol = n_kmers - 1 - k0p;
-            const int e0p = bk - 2 - k0p;
+            const int ol = n_kmers - 1 - k0, e0p = bk - 2 - k0;
+            int lop, hip;  // band bk's computed offsets
+            band_range(k0, e0p, n_events, n_kmers, lop, hip);
             if (t == sl_last && ol >= lop && ol < hip && in_bounds(e0p - ol, n_events, a.counters))
                 lastc[e0p - ol] = s1;
         }
@@ -882,9 +883,6 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             lp = left;
             s1 = best;
             from_p = from;
-            k0p = k0;
-            lop = lo;
-            hip = hi;
         }
     };
     // The state an optimistic chunk starts from (band bb-1's placement, score,
@@ -905,7 +903,7 @@ __device__ void fill_chain(const CoreArgs& a, const ReadDesc& r, ChainSmem<kRing
             return;
         }
         if (named_bar_any(kBarChain, kSlots, dirty)) {
-            k0 = k0p = sv_k0;
+            k0 = sv_k0;
             s1 = sv_s1;
             lp = sv_lp;
             from_p = sv_from;
