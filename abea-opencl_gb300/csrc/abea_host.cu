@@ -2093,7 +2093,10 @@ extern "C" const char* abea_internal_set_error(const char* msg) {
 // The batched form's heuristic wide-shape threshold for a batch of reads with
 // these band counts on `blocks` resident blocks (no device needed): for tests
 // and for callers who size batches.  INT64_MAX = no wide read; -1 = bad input.
-extern "C" int64_t abea_internal_wide_threshold(const int64_t* n_bands, int32_t n_reads, int32_t blocks) {
+// The heuristic on band counts alone (host code, for tests); ck (optional) marks
+// the reads whose trace is not kept (checkpointed), which stay on the warp shape.
+extern "C" int64_t abea_internal_wide_threshold_ck(const int64_t* n_bands, const int32_t* ck, int32_t n_reads,
+                                                   int32_t blocks) {
     if (n_reads < 0 || blocks < 1 || (n_reads > 0 && !n_bands)) return -1;
     abea_batch b;
     b.n_reads = n_reads;
@@ -2101,6 +2104,7 @@ extern "C" int64_t abea_internal_wide_threshold(const int64_t* n_bands, int32_t 
     for (int32_t i = 0; i < n_reads; ++i) {
         if (n_bands[i] < 0) return -1;
         b.reads[(size_t)i].n_bands = (int32_t)std::min<int64_t>(n_bands[i], INT32_MAX);
+        b.reads[(size_t)i].ck = ck && ck[i] ? 1 : 0;
     }
     b.order.resize((size_t)n_reads);
     std::iota(b.order.begin(), b.order.end(), 0);
@@ -2108,4 +2112,8 @@ extern "C" int64_t abea_internal_wide_threshold(const int64_t* n_bands, int32_t 
         return b.reads[(size_t)x].n_bands > b.reads[(size_t)y].n_bands;
     });
     return heuristic_threshold(&b, blocks);
+}
+
+extern "C" int64_t abea_internal_wide_threshold(const int64_t* n_bands, int32_t n_reads, int32_t blocks) {
+    return abea_internal_wide_threshold_ck(n_bands, nullptr, n_reads, blocks);
 }

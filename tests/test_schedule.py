@@ -65,3 +65,22 @@ def test_fewer_reads_than_blocks_and_edge_inputs():
     assert wide_threshold([]) >= 2**62                 # nothing to do
     assert wide_threshold([10, -1]) == -1              # bad input
     assert wide_threshold([10], blocks=0) == -1
+
+
+def test_checkpointed_reads_keep_the_split():
+    """A latency-bound batch with checkpointed reads (trace over the budget): those
+    run on the warp shape and would start last behind every wide read, so the
+    heuristic keeps at most one wide read per block and never a checkpointed one."""
+    if not os.path.exists(abea.LIB_PATH):
+        abea.build()
+    f = abea.lib().abea_internal_wide_threshold_ck
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32]
+    f.restype = C.c_int64
+    from abea_gb300 import synth
+    nb = np.ascontiguousarray(synth.make_batch("f5c_batch", seed=1).n_bands(), dtype=np.int64)
+    ck = np.zeros(len(nb), dtype=np.int32)
+    assert f(nb.ctypes.data, ck.ctypes.data, len(nb), 152) == 1          # no checkpointed read: every read wide
+    ck[np.argsort(-nb)[200:210]] = 1                                     # ten mid-length reads checkpointed
+    thr = f(nb.ctypes.data, ck.ctypes.data, len(nb), 152)
+    k = int(np.sum((nb >= thr) & (ck == 0)))
+    assert thr > 1 and 0 < k < 152, (thr, k)
